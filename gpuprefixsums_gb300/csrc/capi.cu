@@ -1,0 +1,354 @@
+// C ABI of the scan library (declared in include/gps.h).
+//
+// A plan plays the part of one constructed reference dispatcher
+// (ChainedScanDecoupledLookbackDispatcher / ReduceThenScanDispatcher): it is
+// created for a maximum size and owns the scratch memory the kernels need.
+// Errors are returned as gps_status and described by gps_last_error(); the
+// reference has no error reporting beyond printf
+// (ChainedScanDecoupledLookbackDispatcher.cuh:117-120).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "gps_internal.h"
+
+struct gps_plan_s {
+    gps_algo algo;
+    gps_dtype dtype;
+    uint64_t max_n;
+    int device;
+    int num_sms;
+    uint32_t tile_elems;
+    uint64_t capacity_tiles;
+    void* scratch;        // WsHeader, then carry slots, then descriptors / tile sums
+    size_t scratch_bytes;
+    gps::WsHeader* hdr;
+    void* carries;        // two elements (host-array scans)
+    void* area;
+    uint64_t wait_budget_ns;
+    gps::StallConfig stall;
+    gps::LaunchInfo last_launch;
+    // Staging for gps_scan_host, created on first use.
+    void* stage[2];
+    uint64_t stage_elems;
+    cudaStream_t copy_in, compute, copy_out;
+    cudaEvent_t ev_loaded[2], ev_scanned[2], ev_free[2], ev_start, ev_done;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gps_status fail(gps_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+gps_status cuda_fail(cudaError_t err, const char* what) {
+    return fail(GPS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
+}
+
+constexpr size_t kHeaderBytes = sizeof(gps::WsHeader);
+constexpr size_t kCarryBytes = 128;  // two carry slots, padded to a line
+constexpr uint64_t kDefaultBudgetNs = 1000000000ull;
+
+size_t desc_bytes(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 16 : 8; }
+
+bool valid_dtype(int d) { return d == GPS_DTYPE_U32 || d == GPS_DTYPE_U64; }
+bool valid_algo(int a) { return a == GPS_ALGO_CSDL || a == GPS_ALGO_RTS; }
+bool valid_kind(int k) { return k == GPS_SCAN_EXCLUSIVE || k == GPS_SCAN_INCLUSIVE; }
+
+gps_status check_device(const gps_plan_s* p) {
+    int dev = -1;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaGetDevice");
+    if (dev != p->device)
+        return fail(GPS_ERR_WRONG_DEVICE, "plan was created on device %d but device %d is current", p->device, dev);
+    return GPS_OK;
+}
+
+// Device-side launch of one scan of n elements (n >= 1, already validated).
+gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out, uint64_t n, const void* carry_in,
+                       void* carry_out, cudaStream_t stream) {
+    gps::ScanArgs a{};
+    a.in = in;
+    a.out = out;
+    a.n = n;
+    a.num_tiles = static_cast<uint32_t>((n + p->tile_elems - 1) / p->tile_elems);
+    a.hdr = p->hdr;
+    a.desc = p->area;
+    a.spine = nullptr;
+    a.carry_in = carry_in;
+    a.carry_out = carry_out;
+    a.wait_budget_ns = p->wait_budget_ns;
+    a.stall = p->stall;
+    cudaError_t err;
+    if (p->algo == GPS_ALGO_CSDL) {
+        err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0, a, p->num_sms, stream, &p->last_launch);
+    } else {
+        err = gps::launch_rts(p->dtype, inclusive, a, p->area, p->num_sms, stream, &p->last_launch);
+    }
+    if (err != cudaSuccess) return cuda_fail(err, "scan launch");
+    return GPS_OK;
+}
+
+}  // namespace
+
+namespace gps {
+size_t dtype_size(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 8 : 4; }
+}  // namespace gps
+
+extern "C" {
+
+int gps_version(void) { return 10000; }
+
+const char* gps_status_string(gps_status status) {
+    switch (status) {
+        case GPS_OK: return "GPS_OK";
+        case GPS_ERR_INVALID_ARGUMENT: return "GPS_ERR_INVALID_ARGUMENT";
+        case GPS_ERR_SIZE_EXCEEDS_PLAN: return "GPS_ERR_SIZE_EXCEEDS_PLAN";
+        case GPS_ERR_CUDA: return "GPS_ERR_CUDA";
+        case GPS_ERR_TIMEOUT: return "GPS_ERR_TIMEOUT";
+        case GPS_ERR_UNSUPPORTED: return "GPS_ERR_UNSUPPORTED";
+        case GPS_ERR_OUT_OF_MEMORY: return "GPS_ERR_OUT_OF_MEMORY";
+        case GPS_ERR_WRONG_DEVICE: return "GPS_ERR_WRONG_DEVICE";
+    }
+    return "GPS_ERR_UNKNOWN";
+}
+
+const char* gps_last_error(void) { return g_last_error.c_str(); }
+
+gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, uint64_t max_n) {
+    if (out_plan == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "out_plan is NULL");
+    *out_plan = nullptr;
+    if (!valid_algo(algo)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown algorithm %d", static_cast<int>(algo));
+    if (!valid_dtype(dtype)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown dtype %d", static_cast<int>(dtype));
+    if (max_n == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "max_n must be at least 1");
+    const uint32_t tile = algo == GPS_ALGO_CSDL ? gps::csdl_tile_elems(dtype) : gps::rts_tile_elems(dtype);
+    const uint64_t tiles = (max_n + tile - 1) / tile;
+    if (tiles >= (1ull << 31))
+        return fail(GPS_ERR_INVALID_ARGUMENT, "max_n %llu needs %llu tiles; the limit is 2^31 - 1",
+                    static_cast<unsigned long long>(max_n), static_cast<unsigned long long>(tiles));
+
+    gps_plan_s* p = new (std::nothrow) gps_plan_s();
+    if (p == nullptr) return fail(GPS_ERR_OUT_OF_MEMORY, "host allocation failed");
+    p->algo = algo;
+    p->dtype = dtype;
+    p->max_n = max_n;
+    p->tile_elems = tile;
+    p->capacity_tiles = tiles;
+    p->wait_budget_ns = kDefaultBudgetNs;
+    cudaError_t err = cudaGetDevice(&p->device);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+    if (err != cudaSuccess) {
+        delete p;
+        return cuda_fail(err, "device query");
+    }
+    const size_t per_tile = algo == GPS_ALGO_CSDL ? desc_bytes(dtype) : gps::dtype_size(dtype);
+    p->scratch_bytes = kHeaderBytes + kCarryBytes + tiles * per_tile;
+    err = cudaMalloc(&p->scratch, p->scratch_bytes);
+    if (err != cudaSuccess) {
+        delete p;
+        return fail(err == cudaErrorMemoryAllocation ? GPS_ERR_OUT_OF_MEMORY : GPS_ERR_CUDA, "cudaMalloc(%zu): %s",
+                    p->scratch_bytes, cudaGetErrorString(err));
+    }
+    p->hdr = static_cast<gps::WsHeader*>(p->scratch);
+    p->carries = static_cast<char*>(p->scratch) + kHeaderBytes;
+    p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
+    gps::WsHeader h{};
+    h.epoch = 1;
+    h.capacity_tiles = tiles;
+    err = cudaMemset(p->scratch, 0, p->scratch_bytes);
+    if (err == cudaSuccess) err = cudaMemcpy(p->hdr, &h, sizeof(h), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaDeviceSynchronize();
+    if (err != cudaSuccess) {
+        cudaFree(p->scratch);
+        delete p;
+        return cuda_fail(err, "scratch initialisation");
+    }
+    *out_plan = p;
+    return GPS_OK;
+}
+
+gps_status gps_plan_destroy(gps_plan p) {
+    if (p == nullptr) return GPS_OK;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(p->device);
+    cudaError_t err = cudaFree(p->scratch);
+    for (int b = 0; b < 2; ++b) {
+        if (p->stage[b]) cudaFree(p->stage[b]);
+        if (p->ev_loaded[b]) cudaEventDestroy(p->ev_loaded[b]);
+        if (p->ev_scanned[b]) cudaEventDestroy(p->ev_scanned[b]);
+        if (p->ev_free[b]) cudaEventDestroy(p->ev_free[b]);
+    }
+    if (p->ev_start) cudaEventDestroy(p->ev_start);
+    if (p->ev_done) cudaEventDestroy(p->ev_done);
+    if (p->copy_in) cudaStreamDestroy(p->copy_in);
+    if (p->compute) cudaStreamDestroy(p->compute);
+    if (p->copy_out) cudaStreamDestroy(p->copy_out);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete p;
+    if (err != cudaSuccess) return cuda_fail(err, "cudaFree");
+    return GPS_OK;
+}
+
+gps_status gps_plan_scratch_bytes(gps_plan p, size_t* out_bytes) {
+    if (p == nullptr || out_bytes == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out_bytes = p->scratch_bytes;
+    return GPS_OK;
+}
+
+gps_status gps_scan(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n, gps_stream_t stream) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
+    if (n == 0) return GPS_OK;
+    if (n > p->max_n)
+        return fail(GPS_ERR_SIZE_EXCEEDS_PLAN, "requested size %llu exceeds the plan's maximum %llu",
+                    static_cast<unsigned long long>(n), static_cast<unsigned long long>(p->max_n));
+    if (d_in == nullptr || d_out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL data pointer");
+    const size_t es = gps::dtype_size(p->dtype);
+    const uintptr_t i = reinterpret_cast<uintptr_t>(d_in), o = reinterpret_cast<uintptr_t>(d_out);
+    if ((i % es) != 0 || (o % es) != 0)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "pointers must be aligned to the %zu-byte element size", es);
+    const uint64_t bytes = n * es;
+    if (i != o && i < o + bytes && o < i + bytes)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "input and output overlap without being identical");
+    gps_status st = check_device(p);
+    if (st != GPS_OK) return st;
+    return launch_scan(p, kind == GPS_SCAN_INCLUSIVE, d_in, d_out, n, nullptr, nullptr,
+                       reinterpret_cast<cudaStream_t>(stream));
+}
+
+gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void* h_out, uint64_t n,
+                         gps_stream_t stream) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
+    if (n == 0) return GPS_OK;
+    if (h_in == nullptr || h_out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL data pointer");
+    gps_status st = check_device(p);
+    if (st != GPS_OK) return st;
+    const size_t es = gps::dtype_size(p->dtype);
+    cudaError_t err = cudaSuccess;
+    if (p->stage[0] == nullptr) {
+        // Chunk: up to 2^24 elements, whole tiles, within the plan's size.
+        uint64_t chunk = std::min<uint64_t>(p->max_n, 1ull << 24);
+        if (chunk > p->tile_elems) chunk -= chunk % p->tile_elems;
+        for (int b = 0; b < 2 && err == cudaSuccess; ++b) err = cudaMalloc(&p->stage[b], chunk * es);
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->copy_in, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->compute, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->copy_out, cudaStreamNonBlocking);
+        for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+            err = cudaEventCreateWithFlags(&p->ev_loaded[b], cudaEventDisableTiming);
+            if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_scanned[b], cudaEventDisableTiming);
+            if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_free[b], cudaEventDisableTiming);
+        }
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming);
+        if (err != cudaSuccess) return cuda_fail(err, "host-scan staging setup");
+        p->stage_elems = chunk;
+    }
+    cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
+    const bool inclusive = kind == GPS_SCAN_INCLUSIVE;
+    char* carry = static_cast<char*>(p->carries);
+    // Work queued on the user's stream before this call comes first.
+    err = cudaEventRecord(p->ev_start, user);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(p->copy_in, p->ev_start, 0);
+    const uint64_t chunks = (n + p->stage_elems - 1) / p->stage_elems;
+    for (uint64_t k = 0; k < chunks && err == cudaSuccess; ++k) {
+        const int b = static_cast<int>(k & 1);
+        const uint64_t off = k * p->stage_elems;
+        const uint64_t cnt = std::min<uint64_t>(p->stage_elems, n - off);
+        if (k >= 2) err = cudaStreamWaitEvent(p->copy_in, p->ev_free[b], 0);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(p->stage[b], static_cast<const char*>(h_in) + off * es, cnt * es,
+                                  cudaMemcpyHostToDevice, p->copy_in);
+        if (err == cudaSuccess) err = cudaEventRecord(p->ev_loaded[b], p->copy_in);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(p->compute, p->ev_loaded[b], 0);
+        if (err != cudaSuccess) break;
+        const void* cin = k == 0 ? nullptr : carry + ((k - 1) & 1) * 64;
+        void* cout = carry + (k & 1) * 64;
+        st = launch_scan(p, inclusive, p->stage[b], p->stage[b], cnt, cin, cout, p->compute);
+        if (st != GPS_OK) return st;
+        err = cudaEventRecord(p->ev_scanned[b], p->compute);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(p->copy_out, p->ev_scanned[b], 0);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(static_cast<char*>(h_out) + off * es, p->stage[b], cnt * es, cudaMemcpyDeviceToHost,
+                                  p->copy_out);
+        if (err == cudaSuccess) err = cudaEventRecord(p->ev_free[b], p->copy_out);
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(p->ev_done, p->copy_out);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(user, p->ev_done, 0);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(user);
+    if (err != cudaSuccess) return cuda_fail(err, "host-array scan");
+    return GPS_OK;
+}
+
+gps_status gps_plan_check(gps_plan p, gps_stream_t stream) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    cudaError_t err = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+    if (err != cudaSuccess) return cuda_fail(err, "cudaStreamSynchronize");
+    uint32_t flags = 0;
+    err = cudaMemcpy(&flags, &p->hdr->error_flags, sizeof(flags), cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "reading device error flags");
+    if (flags != 0) {
+        const uint32_t zero = 0;
+        err = cudaMemcpy(&p->hdr->error_flags, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+        if (err != cudaSuccess) return cuda_fail(err, "clearing device error flags");
+        return fail(GPS_ERR_TIMEOUT, "a device-side wait exceeded its budget (flags 0x%x)", flags);
+    }
+    return GPS_OK;
+}
+
+gps_status gps_plan_set_wait_budget(gps_plan p, uint64_t budget_ns) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (budget_ns == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "budget must be positive");
+    p->wait_budget_ns = budget_ns;
+    return GPS_OK;
+}
+
+gps_status gps_plan_set_stall(gps_plan p, uint32_t mode, uint32_t period, uint32_t seed, uint32_t delay_ns,
+                              uint32_t fallback_polls) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (mode > 2) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown stall mode %u", mode);
+    if (mode != 0 && p->algo != GPS_ALGO_CSDL)
+        return fail(GPS_ERR_UNSUPPORTED, "forced-stall mode applies to the chained scan only");
+    if (mode != 0 && period == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "period must be positive");
+    if (delay_ns > 1000000000u) return fail(GPS_ERR_INVALID_ARGUMENT, "delay %u ns exceeds one second", delay_ns);
+    p->stall = gps::StallConfig{mode, period, seed, delay_ns, fallback_polls, 0};
+    return GPS_OK;
+}
+
+gps_status gps_plan_stats(gps_plan p, gps_stream_t stream, gps_lookback_stats* out) {
+    if (p == nullptr || out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaError_t err = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+    gps::WsHeader h{};
+    if (err == cudaSuccess) err = cudaMemcpy(&h, p->hdr, sizeof(h), cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "reading statistics");
+    out->polls = h.stat_polls;
+    out->fallbacks = h.stat_fallbacks;
+    out->inserts = h.stat_inserts;
+    out->stalls = h.stat_stalls;
+    return GPS_OK;
+}
+
+gps_status gps_plan_geometry(gps_plan p, uint64_t n, uint32_t* tile_elems, uint32_t* grid, uint32_t* launches) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (tile_elems) *tile_elems = p->tile_elems;
+    if (grid) *grid = static_cast<uint32_t>(p->last_launch.grid);
+    if (launches) *launches = n == 0 ? 0u : (p->algo == GPS_ALGO_CSDL ? 1u : 3u);
+    return GPS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// Comparison bar for the benchmark: CUB's DeviceScan (CCCL of the CUDA
+// toolkit) compiled for sm_103a, as the reference's CubDispatcher times it
+// (GPUPrefixSumsCUDA/CubDispatcher.cuh:32-76). Built as libgps_cub.so, apart
+// from the scan library; nothing in libgps.so calls CUB.
+#include <cub/device/device_scan.cuh>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+extern "C" {
+
+// Query (temp == nullptr) or run CUB's exclusive / inclusive sum of n u32.
+int gps_cub_scan_u32(int inclusive, const void* in, void* out, uint64_t n, void* temp, size_t* temp_bytes,
+                     cudaStream_t stream) {
+    const uint32_t* i = static_cast<const uint32_t*>(in);
+    uint32_t* o = static_cast<uint32_t*>(out);
+    cudaError_t err;
+    if (inclusive)
+        err = cub::DeviceScan::InclusiveSum(temp, *temp_bytes, i, o, static_cast<int64_t>(n), stream);
+    else
+        err = cub::DeviceScan::ExclusiveSum(temp, *temp_bytes, i, o, static_cast<int64_t>(n), stream);
+    return static_cast<int>(err);
+}
+
+int gps_cub_scan_u64(int inclusive, const void* in, void* out, uint64_t n, void* temp, size_t* temp_bytes,
+                     cudaStream_t stream) {
+    const uint64_t* i = static_cast<const uint64_t*>(in);
+    uint64_t* o = static_cast<uint64_t*>(out);
+    cudaError_t err;
+    if (inclusive)
+        err = cub::DeviceScan::InclusiveSum(temp, *temp_bytes, i, o, static_cast<int64_t>(n), stream);
+    else
+        err = cub::DeviceScan::ExclusiveSum(temp, *temp_bytes, i, o, static_cast<int64_t>(n), stream);
+    return static_cast<int>(err);
+}
+}

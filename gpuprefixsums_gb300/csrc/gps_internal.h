@@ -1,0 +1,108 @@
+// Internal definitions shared by the scan kernels and the C ABI layer:
+// the device workspace header, the tile-descriptor encodings and the kernel
+// argument block.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gps.h"
+
+namespace gps {
+
+// Tile ids handed out by the producer; kTileEnd marks "no more tiles".
+constexpr uint32_t kTileEnd = 0xFFFFFFFFu;
+
+// Epochs are 30 bits wide so that they fit beside a 32-bit value in a 64-bit
+// descriptor. Epoch 0 never occurs, so a zeroed workspace is "not ready".
+constexpr uint32_t kEpochMask = 0x3FFFFFFFu;
+
+// Descriptor status (two bits), as in the decoupled-lookback scheme:
+// not ready / tile aggregate only / inclusive prefix through this tile.
+enum DescStatus : uint32_t { kNotReady = 0, kAggregate = 1, kInclusive = 2 };
+
+// Bits of WsHeader::error_flags.
+enum ErrFlag : uint32_t {
+    kErrLookbackTimeout = 1u,  // a lookback spin ran past its wait budget
+    kErrPipelineTimeout = 2u,  // an mbarrier wait ran past its wait budget
+    kErrStallTimeout = 4u,     // a forced-stall wait ran past its wait budget
+};
+
+// Device-resident state of one plan. Zeroed at plan creation, then epoch=1.
+// tile_counter / exit_counter are returned to zero by the last CTA of every
+// launch, and the same CTA advances the epoch, so consecutive launches need no
+// memset and a launch can be replayed from a CUDA graph.
+struct alignas(128) WsHeader {
+    uint32_t tile_counter;
+    uint32_t exit_counter;
+    uint32_t epoch;
+    uint32_t error_flags;
+    unsigned long long capacity_tiles;  // descriptor slots that follow
+    unsigned long long stat_polls;      // lookback windows re-polled (stats mode)
+    unsigned long long stat_fallbacks;  // predecessor tiles re-reduced
+    unsigned long long stat_inserts;    // fallback aggregates that won the CAS
+    unsigned long long stat_stalls;     // tiles that were made to stall
+};
+static_assert(sizeof(WsHeader) == 128, "header is one 128-byte line");
+
+// Forced-stall test mode (EmulatedDeadlocking-style).
+//  mode 0: off.
+//  mode 1: every tile with (t % period) == 0 stalls (the reference pattern).
+//  mode 2: tiles selected by a seeded hash with probability 1/period stall.
+// A stalled tile withholds its aggregate for up to delay_ns or until a
+// successor re-reduces its input and inserts the aggregate for it
+// (fallback_polls > 0 enables that fallback after this many empty polls).
+struct StallConfig {
+    uint32_t mode;
+    uint32_t period;
+    uint32_t seed;
+    uint32_t delay_ns;
+    uint32_t fallback_polls;
+    uint32_t pad_;
+};
+
+enum class PrefixMode : int { Lookback = 0, Spine = 1 };
+
+struct ScanArgs {
+    const void* in;
+    void* out;
+    uint64_t n;
+    uint32_t num_tiles;
+    uint32_t pad_;
+    WsHeader* hdr;       // plan state (counters, epoch, error flags)
+    void* desc;          // tile descriptors (lookback)
+    const void* spine;   // inclusive scan of tile sums (reduce-then-scan)
+    const void* carry_in;  // optional: one element added to every output
+    void* carry_out;       // optional: receives carry_in + sum of all n inputs
+    uint64_t wait_budget_ns;
+    StallConfig stall;
+};
+
+// Kernel geometry shared by host and device: 64 bytes of input per consumer
+// thread, W consumer warps and one producer warp per CTA.
+template <typename T, int W>
+struct TileShape {
+    static constexpr int kItems = 64 / static_cast<int>(sizeof(T));
+    static constexpr int kConsumers = W * 32;
+    static constexpr int kTile = kConsumers * kItems;
+    static constexpr int kThreads = kConsumers + 32;
+};
+
+// ------------------------------------------------------------ launchers
+// Each returns the launch status; they never synchronize.
+struct LaunchInfo {
+    int grid;
+    int block;
+    size_t smem;
+};
+
+cudaError_t launch_csdl(gps_dtype dtype, bool inclusive, bool stall_mode, const ScanArgs& a,
+                        int num_sms, cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_rts(gps_dtype dtype, bool inclusive, const ScanArgs& a, void* tile_sums,
+                       int num_sms, cudaStream_t stream, LaunchInfo* info);
+
+uint32_t csdl_tile_elems(gps_dtype dtype);
+uint32_t rts_tile_elems(gps_dtype dtype);
+size_t dtype_size(gps_dtype dtype);
+
+}  // namespace gps

@@ -1,0 +1,188 @@
+// Inline-PTX helpers for sm_103a: mbarriers, bulk (TMA) copies between global
+// and shared memory, async-proxy fences, gpu-scope relaxed 64/128-bit accesses
+// for the inter-tile descriptors, and the nanosecond global timer that bounds
+// every device-side wait.
+#pragma once
+#include <cstdint>
+
+namespace gps {
+namespace ptx {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint32_t lane_id() {
+    uint32_t l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------- mbarrier
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete. Gives up once
+// `deadline_ns` of the global timer has passed and returns false; the caller
+// records the timeout. A bulk copy whose addresses are valid always
+// completes, so in practice this only expires on a hung producer.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t deadline_ns) {
+    uint32_t polls = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if ((++polls & 63u) == 0 && global_timer_ns() > deadline_ns) return false;
+    }
+    return true;
+}
+
+// ------------------------------------------------------- bulk (TMA) copies
+// global -> shared, completion counted on an mbarrier (bytes).
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, uint32_t bytes,
+                                          uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(smem_dst)),
+        "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// shared -> global, tracked as a bulk async-group of the issuing thread.
+__device__ __forceinline__ void bulk_store(void* gmem_dst, const void* smem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gmem_dst),
+                 "r"(smem_addr(smem_src)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() {
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// Wait until at most N of this thread's bulk groups still read shared memory.
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void bulk_wait_all() {
+    asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Generic-proxy shared-memory writes become visible to the async proxy (bulk
+// stores) after this fence.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Named barrier over a subset of the CTA's warps.
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t threads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// --------------------------------------------- gpu-scope descriptor access
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t atom_cas_u64(uint64_t* p, uint64_t cmp, uint64_t val) {
+    uint64_t old;
+    asm volatile("atom.relaxed.gpu.global.cas.b64 %0, [%1], %2, %3;"
+                 : "=l"(old)
+                 : "l"(p), "l"(cmp), "l"(val)
+                 : "memory");
+    return old;
+}
+
+// 128-bit descriptors: {lo = payload bits, hi = status/epoch word}, accessed
+// as one single-copy-atomic .b128 operation.
+struct u64x2 {
+    uint64_t lo, hi;
+};
+
+__device__ __forceinline__ u64x2 ld_relaxed_b128(const u64x2* p) {
+    u64x2 r;
+    asm volatile(
+        "{\n\t.reg .b128 v;\n\t"
+        "ld.relaxed.gpu.global.b128 v, [%2];\n\t"
+        "mov.b128 {%0, %1}, v;\n\t}"
+        : "=l"(r.lo), "=l"(r.hi)
+        : "l"(p)
+        : "memory");
+    return r;
+}
+
+__device__ __forceinline__ void st_relaxed_b128(u64x2* p, u64x2 v) {
+    asm volatile(
+        "{\n\t.reg .b128 v;\n\t"
+        "mov.b128 v, {%1, %2};\n\t"
+        "st.relaxed.gpu.global.b128 [%0], v;\n\t}" ::"l"(p),
+        "l"(v.lo), "l"(v.hi)
+        : "memory");
+}
+
+// Compare-and-swap of a whole 128-bit descriptor; returns the old value.
+__device__ __forceinline__ u64x2 atom_cas_b128(u64x2* p, u64x2 cmp, u64x2 val) {
+    u64x2 old;
+    asm volatile(
+        "{\n\t.reg .b128 c, v, o;\n\t"
+        "mov.b128 c, {%3, %4};\n\t"
+        "mov.b128 v, {%5, %6};\n\t"
+        "atom.relaxed.gpu.global.cas.b128 o, [%2], c, v;\n\t"
+        "mov.b128 {%0, %1}, o;\n\t}"
+        : "=l"(old.lo), "=l"(old.hi)
+        : "l"(p), "l"(cmp.lo), "l"(cmp.hi), "l"(val.lo), "l"(val.hi)
+        : "memory");
+    return old;
+}
+
+// Streaming 16-byte global accesses for the plain (non-bulk) paths.
+__device__ __forceinline__ uint4 ld_stream_v4(const void* p) {
+    uint4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+}  // namespace ptx
+}  // namespace gps

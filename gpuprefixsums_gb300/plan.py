@@ -1,0 +1,120 @@
+"""Python view of a scan plan (``gps_plan`` in ``include/gps.h``).
+
+A plan corresponds to one constructed reference dispatcher
+(``ChainedScanDecoupledLookbackDispatcher(maxSize)`` or
+``ReduceThenScanDispatcher(maxSize)``): algorithm, element type and maximum
+size are fixed, scratch memory is owned. Data are torch CUDA tensors (or raw
+device pointers); every call goes through ``libgps.so``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import _lib
+from ._lib import check, lib
+
+_ALGOS = {"csdl": _lib.ALGO_CSDL, "rts": _lib.ALGO_RTS}
+_DTYPES = {"u32": (_lib.DTYPE_U32, 4), "u64": (_lib.DTYPE_U64, 8)}
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Plan:
+    def __init__(self, algo: str = "csdl", dtype: str = "u32", max_n: int = 1 << 20):
+        if algo not in _ALGOS:
+            raise ValueError(f"algo must be one of {sorted(_ALGOS)}")
+        if dtype not in _DTYPES:
+            raise ValueError(f"dtype must be one of {sorted(_DTYPES)}")
+        self.algo, self.dtype, self.max_n = algo, dtype, int(max_n)
+        self.elem_size = _DTYPES[dtype][1]
+        h = ctypes.c_void_p()
+        check(lib.gps_plan_create(ctypes.byref(h), _ALGOS[algo], _DTYPES[dtype][0], self.max_n), "gps_plan_create")
+        self._h = h
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            check(lib.gps_plan_destroy(self._h), "gps_plan_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    # -- scans
+    def scan_ptr(self, in_ptr: int, out_ptr: int, n: int, inclusive: bool = False, stream=None) -> None:
+        kind = _lib.INCLUSIVE if inclusive else _lib.EXCLUSIVE
+        check(lib.gps_scan(self._h, kind, ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr), int(n),
+                           ctypes.c_void_p(_stream_handle(stream))), "gps_scan")
+
+    def scan(self, x, out=None, inclusive: bool = False, n: int | None = None, stream=None):
+        """Scan the first n elements of CUDA tensor x into out (allocated if None;
+        out may be x for an in-place scan). Bits are taken as unsigned."""
+        if x.element_size() != self.elem_size:
+            raise TypeError(f"plan is {self.dtype}; tensor has {x.element_size()}-byte elements")
+        if not (x.is_cuda and x.is_contiguous()):
+            raise ValueError("x must be a contiguous CUDA tensor")
+        if out is None:
+            import torch
+            out = torch.empty_like(x)
+        if out.element_size() != self.elem_size or not out.is_contiguous():
+            raise ValueError("out must be contiguous with the plan's element size")
+        count = x.numel() if n is None else int(n)
+        if count > x.numel() or count > out.numel():
+            raise ValueError("n exceeds the tensor length")
+        self.scan_ptr(x.data_ptr(), out.data_ptr(), count, inclusive, stream)
+        return out
+
+    def scan_host(self, h_in: int, h_out: int, n: int, inclusive: bool = False, stream=None) -> None:
+        """Scan n elements of a host array (pointers; pinned memory for speed)."""
+        kind = _lib.INCLUSIVE if inclusive else _lib.EXCLUSIVE
+        check(lib.gps_scan_host(self._h, kind, ctypes.c_void_p(h_in), ctypes.c_void_p(h_out), int(n),
+                                ctypes.c_void_p(_stream_handle(stream))), "gps_scan_host")
+
+    # -- status, test modes, geometry
+    def check(self, stream=None) -> None:
+        check(lib.gps_plan_check(self._h, ctypes.c_void_p(_stream_handle(stream))), "gps_plan_check")
+
+    def check_status(self, stream=None) -> int:
+        return lib.gps_plan_check(self._h, ctypes.c_void_p(_stream_handle(stream)))
+
+    def set_wait_budget(self, budget_ns: int) -> None:
+        check(lib.gps_plan_set_wait_budget(self._h, int(budget_ns)), "gps_plan_set_wait_budget")
+
+    def set_stall(self, mode: int, period: int = 8, seed: int = 0, delay_ns: int = 0, fallback_polls: int = 0) -> None:
+        check(lib.gps_plan_set_stall(self._h, mode, period, seed, delay_ns, fallback_polls), "gps_plan_set_stall")
+
+    def stats(self, stream=None) -> dict:
+        s = _lib.LookbackStats()
+        check(lib.gps_plan_stats(self._h, ctypes.c_void_p(_stream_handle(stream)), ctypes.byref(s)), "gps_plan_stats")
+        return {"polls": s.polls, "fallbacks": s.fallbacks, "inserts": s.inserts, "stalls": s.stalls}
+
+    def geometry(self, n: int) -> dict:
+        t, g, l = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib.gps_plan_geometry(self._h, int(n), ctypes.byref(t), ctypes.byref(g), ctypes.byref(l)),
+              "gps_plan_geometry")
+        return {"tile_elems": t.value, "grid": g.value, "launches": l.value}
+
+    def scratch_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        check(lib.gps_plan_scratch_bytes(self._h, ctypes.byref(b)), "gps_plan_scratch_bytes")
+        return b.value

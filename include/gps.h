@@ -1,0 +1,166 @@
+/*
+ * gps.h -- C ABI of the GB300 device-wide prefix-scan library.
+ *
+ * The reference (b0nes164/GPUPrefixSums, CUDA part) exposes its scans only as
+ * header-only C++ dispatcher classes that own their device buffers:
+ *
+ *   ChainedScanDecoupledLookbackDispatcher(uint32_t maxSize)
+ *       GPUPrefixSumsCUDA/ChainedScanDecoupledLookbackDispatcher.cuh:28-34
+ *   ReduceThenScanDispatcher(uint32_t maxSize)
+ *       GPUPrefixSumsCUDA/ReduceThenScanDispatcher.cuh:27-32
+ *   private DispatchKernelsExclusive / DispatchKernelsInclusive(uint32_t size)
+ *       ChainedScanDecoupledLookbackDispatcher.cuh:177-195,
+ *       ReduceThenScanDispatcher.cuh:171-187
+ *
+ * This header is the thin C layer those classes sit on here (see
+ * include/gps_compat/ for the classes with the reference's names). A plan
+ * stands for one constructed dispatcher: it fixes the algorithm, the element
+ * type and the maximum size, and owns the scratch memory (tile descriptors,
+ * tile sums) that the reference's constructor allocates. Unlike the reference,
+ * the data buffers are the caller's: scans run on any device pointers, in place
+ * or out of place, on any stream, and never write outside [0, n).
+ *
+ * All entry points return a gps_status; none of them synchronizes unless its
+ * comment says so. Device-side waits are bounded: a wait that runs past the
+ * plan's budget records a flag that gps_plan_check() reports as
+ * GPS_ERR_TIMEOUT, and the kernel exits instead of hanging.
+ */
+#ifndef GPS_H_
+#define GPS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* gps_stream_t;
+
+typedef enum gps_status {
+    GPS_OK = 0,
+    GPS_ERR_INVALID_ARGUMENT = 1,
+    /* n larger than the plan's max_n. The reference prints "Error, requested
+     * test size exceeds max initialized size." and returns
+     * (ChainedScanDecoupledLookbackDispatcher.cuh:117-120). */
+    GPS_ERR_SIZE_EXCEEDS_PLAN = 2,
+    GPS_ERR_CUDA = 3,
+    GPS_ERR_TIMEOUT = 4,
+    GPS_ERR_UNSUPPORTED = 5,
+    GPS_ERR_OUT_OF_MEMORY = 6,
+    GPS_ERR_WRONG_DEVICE = 7
+} gps_status;
+
+typedef enum gps_dtype {
+    GPS_DTYPE_U32 = 0, /* uint32_t, sums wrap mod 2^32 (the reference's type) */
+    GPS_DTYPE_U64 = 1  /* uint64_t, sums wrap mod 2^64 */
+} gps_dtype;
+
+typedef enum gps_algo {
+    /* Single-pass chained scan with decoupled lookback
+     * (ChainedScanDecoupledLookback.cuh:79-153). */
+    GPS_ALGO_CSDL = 0,
+    /* Reduce -> spine scan -> propagate, three launches
+     * (ReduceThenScan.cuh:15-161, ReduceThenScanDispatcher.cuh:165-187). */
+    GPS_ALGO_RTS = 1
+} gps_algo;
+
+typedef enum gps_scan_kind {
+    GPS_SCAN_EXCLUSIVE = 0, /* out[i] = in[0] + ... + in[i-1], out[0] = 0 */
+    GPS_SCAN_INCLUSIVE = 1  /* out[i] = in[0] + ... + in[i] */
+} gps_scan_kind;
+
+typedef struct gps_plan_s* gps_plan;
+
+/* Version of this ABI (major*10000 + minor*100 + patch). */
+int gps_version(void);
+
+/* Text for a status code (static storage). */
+const char* gps_status_string(gps_status status);
+
+/* Text of the last error raised on this host thread ("" if none). */
+const char* gps_last_error(void);
+
+/* Creates a plan on the current device for scans of up to max_n elements
+ * (max_n >= 1). Allocates and zeroes the plan's scratch memory with
+ * cudaMalloc; synchronizes the device once.
+ * Replaces: ChainedScanDecoupledLookbackDispatcher(uint32_t maxSize)
+ * (ChainedScanDecoupledLookbackDispatcher.cuh:28-34) and
+ * ReduceThenScanDispatcher(uint32_t maxSize) (ReduceThenScanDispatcher.cuh:27-32). */
+gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, uint64_t max_n);
+
+/* Frees the plan's scratch memory (cudaFree, which synchronizes).
+ * Replaces: ~ChainedScanDecoupledLookbackDispatcher() (:158-163),
+ * ~ReduceThenScanDispatcher() (ReduceThenScanDispatcher.cuh:152-156). */
+gps_status gps_plan_destroy(gps_plan plan);
+
+/* Bytes of device scratch memory the plan holds. */
+gps_status gps_plan_scratch_bytes(gps_plan plan, size_t* out_bytes);
+
+/* Prefix scan of n elements from d_in into d_out on `stream`, asynchronously.
+ * d_in == d_out scans in place (as the reference always does); any other
+ * overlap is rejected. Pointers must be aligned to the element size; 16-byte
+ * aligned pointers take the bulk-copy (TMA) path. Only [0, n) of d_out is
+ * written. n == 0 is a no-op. One plan must not be used by two scans that
+ * can run at the same time (its descriptors and counters are shared).
+ * Replaces: DispatchKernelsExclusive / DispatchKernelsInclusive(uint32_t size)
+ * (ChainedScanDecoupledLookbackDispatcher.cuh:177-195,
+ * ReduceThenScanDispatcher.cuh:171-187), which scan the dispatcher's own
+ * buffer in place. */
+gps_status gps_scan(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                    gps_stream_t stream);
+
+/* Scan of a host array: copies h_in to the device, scans, copies the result
+ * to h_out, in chunks so that the copies in both directions overlap the
+ * scans; returns when h_out is complete (synchronizes `stream`). Host buffers
+ * should be pinned (cudaHostAlloc / cudaHostRegister) for full speed; h_in ==
+ * h_out is allowed. n may exceed the plan's max_n: the plan only bounds the
+ * chunk size. Device staging memory is allocated on first use and kept by
+ * the plan. */
+gps_status gps_scan_host(gps_plan plan, gps_scan_kind kind, const void* h_in, void* h_out,
+                         uint64_t n, gps_stream_t stream);
+
+/* Synchronizes `stream`, then reads and clears the plan's device error
+ * flags: GPS_ERR_TIMEOUT if a bounded device-side wait expired since the last
+ * check (the affected output is then undefined), else GPS_OK. */
+gps_status gps_plan_check(gps_plan plan, gps_stream_t stream);
+
+/* Budget for each device-side wait of this plan's kernels, in nanoseconds
+ * (default 1e9 = one second). */
+gps_status gps_plan_set_wait_budget(gps_plan plan, uint64_t budget_ns);
+
+/* Forced-stall test mode for GPS_ALGO_CSDL, in the style of the reference's
+ * EmulatedDeadlocking (EmulatedDeadlocking.cuh:26-168): selected tiles
+ * withhold their aggregate for up to delay_ns, and, when fallback_polls > 0,
+ * a successor whose lookback sees no progress for that many polls re-reduces
+ * the stalled tile's input and inserts its aggregate with a compare-and-swap.
+ *   mode 0: off; mode 1: tiles with (tile % period) == 0 stall (the
+ *   reference's DEADLOCK_MASK pattern with period 8); mode 2: tiles picked by
+ *   a hash of (seed, tile) with probability 1/period.
+ * delay_ns is at most one second. Results stay exact unless a successor's
+ * wait runs past the plan's budget, which gps_plan_check() reports. */
+gps_status gps_plan_set_stall(gps_plan plan, uint32_t mode, uint32_t period, uint32_t seed,
+                              uint32_t delay_ns, uint32_t fallback_polls);
+
+/* Lookback statistics gathered while forced-stall mode is on. Synchronizes
+ * `stream`. */
+typedef struct gps_lookback_stats {
+    uint64_t polls;     /* lookback windows that had to be re-read */
+    uint64_t fallbacks; /* stalled predecessors re-reduced by a successor */
+    uint64_t inserts;   /* re-reduced aggregates that won the compare-and-swap */
+    uint64_t stalls;    /* tiles that stalled */
+} gps_lookback_stats;
+gps_status gps_plan_stats(gps_plan plan, gps_stream_t stream, gps_lookback_stats* out_stats);
+
+/* Kernel geometry of the plan (for tools and tests): elements per tile of the
+ * main scan kernel, its grid size for a scan of n elements, and the number of
+ * kernel launches one gps_scan of n elements makes. */
+gps_status gps_plan_geometry(gps_plan plan, uint64_t n, uint32_t* tile_elems, uint32_t* grid,
+                             uint32_t* launches);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* GPS_H_ */

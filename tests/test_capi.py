@@ -1,0 +1,75 @@
+"""The C-ABI library on the CPU: it loads, exports every entry point that
+include/*.h declares, and rejects bad arguments before touching the GPU."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+pytestmark = pytest.mark.usefixtures("built")
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"\b(gps_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_the_expected_entry_points():
+    names = declared_functions()
+    for required in ("gps_plan_create", "gps_plan_destroy", "gps_scan", "gps_scan_host", "gps_plan_check"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol():
+    from gpuprefixsums_gb300 import lib
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_bindings_cover_every_declared_symbol():
+    from gpuprefixsums_gb300 import _lib
+    bound = {name for name, _, _ in _lib.SIGNATURES}
+    assert set(declared_functions()) <= bound
+
+
+def test_status_strings_and_version():
+    from gpuprefixsums_gb300 import _lib, lib
+    assert lib.gps_version() >= 10000
+    for code, name in [(0, b"GPS_OK"), (2, b"GPS_ERR_SIZE_EXCEEDS_PLAN"), (4, b"GPS_ERR_TIMEOUT")]:
+        assert lib.gps_status_string(code) == name
+    assert lib.gps_status_string(99) == b"GPS_ERR_UNKNOWN"
+    assert _lib.GPS_ERR_WRONG_DEVICE == 7
+
+
+def test_null_plan_is_rejected_without_a_gpu():
+    from gpuprefixsums_gb300 import _lib, lib
+    assert lib.gps_plan_destroy(None) == _lib.GPS_OK
+    assert lib.gps_scan(None, 0, None, None, 10, None) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert b"plan is NULL" in lib.gps_last_error()
+    assert lib.gps_scan_host(None, 0, None, None, 10, None) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert lib.gps_plan_check(None, None) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert lib.gps_plan_set_wait_budget(None, 5) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert lib.gps_plan_create(None, 0, 0, 10) == _lib.GPS_ERR_INVALID_ARGUMENT
+
+
+def test_plan_create_rejects_bad_arguments_before_any_cuda_call():
+    from gpuprefixsums_gb300 import _lib, lib
+    h = ctypes.c_void_p()
+    assert lib.gps_plan_create(ctypes.byref(h), 9, 0, 10) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert lib.gps_plan_create(ctypes.byref(h), 0, 9, 10) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert lib.gps_plan_create(ctypes.byref(h), 0, 0, 0) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert lib.gps_plan_create(ctypes.byref(h), 0, 0, 1 << 60) == _lib.GPS_ERR_INVALID_ARGUMENT
+    assert h.value is None
+
+
+def test_compat_selftest_was_built():
+    from gpuprefixsums_gb300.build import SELFTEST_BIN
+    assert os.access(SELFTEST_BIN, os.X_OK)
