@@ -155,8 +155,11 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
         delete p;
         return cuda_fail(err, "device query");
     }
+    // Chained scan: one descriptor per tile plus the lookback padding;
+    // reduce-then-scan: one tile sum per tile.
     const size_t per_tile = algo == GPS_ALGO_CSDL ? desc_bytes(dtype) : gps::dtype_size(dtype);
-    p->scratch_bytes = kHeaderBytes + kCarryBytes + tiles * per_tile;
+    const uint64_t slots = algo == GPS_ALGO_CSDL ? tiles + gps::kDescPad : tiles;
+    p->scratch_bytes = kHeaderBytes + kCarryBytes + slots * per_tile;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;
@@ -168,7 +171,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
     gps::WsHeader h{};
     h.epoch = 1;
-    h.capacity_tiles = tiles;
+    h.capacity_tiles = slots;
     err = cudaMemset(p->scratch, 0, p->scratch_bytes);
     if (err == cudaSuccess) err = cudaMemcpy(p->hdr, &h, sizeof(h), cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaDeviceSynchronize();

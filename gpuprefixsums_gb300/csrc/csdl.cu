@@ -6,21 +6,26 @@
 // its descriptors and bump counter with two cudaMemsets per call; here the
 // kernel leaves its workspace ready for the next launch itself.
 #include "launch_util.h"
+#include "scan_l2.cuh"
 #include "scan_pipeline.cuh"
 
 namespace gps {
 
 namespace {
 
-// Tuned shape: 8 consumer warps, 4-deep ring of 16 KB tiles (64 KB of
-// shared memory per CTA, 3 CTAs per SM).
-constexpr int kCsdlWarps = 8;
-constexpr int kCsdlStages = 4;
+// Shape: 4 reduce + 4 finalize warps over 16 KB tiles (4096 u32 / 2048 u64),
+// a 12-deep ring (192 KB of shared memory, one CTA per SM) holding three
+// lookback units of 4 tiles (64 KB) each. One CTA per SM and 64 KB units keep
+// the number of descriptors every lookback reads, and the number of readers,
+// small.
+constexpr int kCsdlWarps = 4;
+constexpr int kCsdlStages = 12;
+constexpr int kCsdlUnit = 4;  // tiles per lookback unit
 
 template <typename T, bool INCL, bool BULK, bool STALL>
 cudaError_t launch_csdl_t(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
     using Shape = TileShape<T, kCsdlWarps>;
-    auto kern = scan_pipeline_kernel<T, kCsdlWarps, kCsdlStages, INCL, BULK, PrefixMode::Lookback, STALL>;
+    auto kern = scan_pipeline_kernel<T, kCsdlWarps, kCsdlStages, kCsdlUnit, INCL, BULK, PrefixMode::Lookback, STALL>;
     constexpr size_t smem = pipeline_smem_bytes<T, kCsdlWarps, kCsdlStages>();
     int occ = 0;
     cudaError_t err = resident_ctas_per_sm(kern, Shape::kThreads, smem, &occ);
@@ -31,18 +36,46 @@ cudaError_t launch_csdl_t(const ScanArgs& a, int num_sms, cudaStream_t stream, L
     return cudaGetLastError();
 }
 
+// L2-buffered kernel (16-byte-aligned buffers): 4 reduce + 4 finalize warps
+// over 16 KB tiles, 4 reduce-pass and 8 scan-pass stages (192 KB, one CTA per
+// SM), lookback units of 4 tiles (64 KB), 6 units in flight per CTA. The
+// queue depth sets how much input waits in L2 between the two passes
+// (152 x 6 x 64 KB at most): measured on GB300 at 2^28 elements, 6 units
+// beat both 4-5 (too shallow to cover the lookback) and 7-8 (the re-loads
+// start missing in L2).
+constexpr int kL2Warps = 4;
+constexpr int kL2RStages = 4;
+constexpr int kL2SStages = 8;
+constexpr int kL2Queue = 6;
+constexpr int kL2Unit = 4;
+
+template <typename T, bool INCL, bool STALL>
+cudaError_t launch_l2_t(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
+    auto kern = scan_l2_kernel<T, kL2Warps, kL2RStages, kL2SStages, kL2Queue, kL2Unit, INCL, STALL>;
+    constexpr size_t smem = l2_smem_bytes<T, kL2Warps, kL2RStages, kL2SStages, kL2Queue>();
+    constexpr int threads = L2Shape<T, kL2Warps>::kThreads;
+    int occ = 0;
+    cudaError_t err = resident_ctas_per_sm(kern, threads, smem, &occ);
+    if (err != cudaSuccess) return err;
+    const uint32_t units = (a.num_tiles + kL2Unit - 1) / kL2Unit;
+    const int grid = persistent_grid(units, occ, num_sms);
+    if (info) *info = LaunchInfo{grid, threads, smem};
+    kern<<<grid, threads, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t dispatch_csdl(bool inclusive, bool stall, const ScanArgs& a, int num_sms, cudaStream_t stream,
                           LaunchInfo* info) {
     const bool bulk = ((reinterpret_cast<uintptr_t>(a.in) | reinterpret_cast<uintptr_t>(a.out)) & 15u) == 0;
-    if (stall) {
-        if (!bulk) return cudaErrorInvalidValue;  // test mode wants aligned buffers
-        return inclusive ? launch_csdl_t<T, true, true, true>(a, num_sms, stream, info)
-                         : launch_csdl_t<T, false, true, true>(a, num_sms, stream, info);
+    if (bulk) {
+        if (stall)
+            return inclusive ? launch_l2_t<T, true, true>(a, num_sms, stream, info)
+                             : launch_l2_t<T, false, true>(a, num_sms, stream, info);
+        return inclusive ? launch_l2_t<T, true, false>(a, num_sms, stream, info)
+                         : launch_l2_t<T, false, false>(a, num_sms, stream, info);
     }
-    if (bulk)
-        return inclusive ? launch_csdl_t<T, true, true, false>(a, num_sms, stream, info)
-                         : launch_csdl_t<T, false, true, false>(a, num_sms, stream, info);
+    if (stall) return cudaErrorInvalidValue;  // test mode wants aligned buffers
     return inclusive ? launch_csdl_t<T, true, false, false>(a, num_sms, stream, info)
                      : launch_csdl_t<T, false, false, false>(a, num_sms, stream, info);
 }

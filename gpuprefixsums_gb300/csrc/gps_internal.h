@@ -17,6 +17,10 @@ constexpr uint32_t kTileEnd = 0xFFFFFFFFu;
 // descriptor. Epoch 0 never occurs, so a zeroed workspace is "not ready".
 constexpr uint32_t kEpochMask = 0x3FFFFFFFu;
 
+// Descriptor slots allocated past the last tile: a lookback window is read in
+// aligned groups of up to 16 slots and may end up to 15 slots after its tile.
+constexpr uint32_t kDescPad = 16;
+
 // Descriptor status (two bits), as in the decoupled-lookback scheme:
 // not ready / tile aggregate only / inclusive prefix through this tile.
 enum DescStatus : uint32_t { kNotReady = 0, kAggregate = 1, kInclusive = 2 };
@@ -78,14 +82,16 @@ struct ScanArgs {
     StallConfig stall;
 };
 
-// Kernel geometry shared by host and device: 64 bytes of input per consumer
-// thread, W consumer warps and one producer warp per CTA.
-template <typename T, int W>
+// Kernel geometry shared by host and device: RW reduce warps and RW finalize
+// warps, each thread of either owning 128 contiguous bytes of the tile, plus
+// one producer warp and kLookbackWarps lookback warps per CTA.
+template <typename T, int RW>
 struct TileShape {
-    static constexpr int kItems = 64 / static_cast<int>(sizeof(T));
-    static constexpr int kConsumers = W * 32;
-    static constexpr int kTile = kConsumers * kItems;
-    static constexpr int kThreads = kConsumers + 32;
+    static constexpr int kItems = 128 / static_cast<int>(sizeof(T));
+    static constexpr int kRoleThreads = RW * 32;
+    static constexpr int kTile = kRoleThreads * kItems;
+    static constexpr int kLookbackWarps = 2;
+    static constexpr int kThreads = 32 * (1 + kLookbackWarps + 2 * RW);
 };
 
 // ------------------------------------------------------------ launchers

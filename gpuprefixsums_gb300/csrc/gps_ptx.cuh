@@ -56,6 +56,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// Non-blocking check that the phase with the given parity has completed.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Waits for the phase with the given parity to complete. Gives up once
 // `deadline_ns` of the global timer has passed and returns false; the caller
 // records the timeout. A bulk copy whose addresses are valid always
@@ -78,6 +91,38 @@ __device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, 
             smem_addr(smem_dst)),
         "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
+}
+
+// L2 cache policies for bulk copies: keep lines that will be read again,
+// drop lines read for the last time.
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// global -> shared with an L2 cache policy.
+__device__ __forceinline__ void bulk_load_hint(void* smem_dst, const void* gmem_src, uint32_t bytes, uint64_t* bar,
+                                               uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_addr(smem_dst)),
+        "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar)), "l"(policy)
+        : "memory");
+}
+
+// shared -> global with an L2 cache policy, tracked as a bulk async-group.
+__device__ __forceinline__ void bulk_store_hint(void* gmem_dst, const void* smem_src, uint32_t bytes,
+                                                uint64_t policy) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group.L2::cache_hint [%0], [%1], %2, %3;" ::"l"(gmem_dst),
+                 "r"(smem_addr(smem_src)), "r"(bytes), "l"(policy)
+                 : "memory");
 }
 
 // shared -> global, tracked as a bulk async-group of the issuing thread.

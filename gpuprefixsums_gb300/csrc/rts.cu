@@ -18,8 +18,8 @@ namespace gps {
 
 namespace {
 
-constexpr int kRtsWarps = 8;
-constexpr int kRtsStages = 4;
+constexpr int kRtsWarps = 4;
+constexpr int kRtsStages = 6;
 constexpr int kReduceThreads = 256;
 constexpr int kSpineThreads = 1024;
 constexpr int kSpineItems = 8;
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kSpineThreads) rts_spine_kernel(T* sums, uint3
 template <typename T, bool INCL, bool BULK>
 cudaError_t launch_propagate(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
     using Shape = TileShape<T, kRtsWarps>;
-    auto kern = scan_pipeline_kernel<T, kRtsWarps, kRtsStages, INCL, BULK, PrefixMode::Spine, false>;
+    auto kern = scan_pipeline_kernel<T, kRtsWarps, kRtsStages, 1, INCL, BULK, PrefixMode::Spine, false>;
     constexpr size_t smem = pipeline_smem_bytes<T, kRtsWarps, kRtsStages>();
     int occ = 0;
     cudaError_t err = resident_ctas_per_sm(kern, Shape::kThreads, smem, &occ);

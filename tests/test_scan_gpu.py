@@ -231,7 +231,8 @@ def test_forced_stall_reference_pattern_with_fallback(cuda, dtype):
         plan.check()
         st = plan.stats()
     assert oracle.validate(x, to_host(out, NP[dtype]), True) == 0
-    assert st["stalls"] >= 300 // 8
+    # Stalls count lookback units (a few tiles each): every 8th of them.
+    assert st["stalls"] >= 300 // (8 * 4)
     assert st["fallbacks"] > 0 and st["inserts"] > 0
 
 
@@ -294,29 +295,54 @@ def _ref():
 
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("inclusive", [False, True])
-def test_reference_kernels_agree_on_config1(cuda, algo, inclusive):
+def test_reference_csdl_agrees_on_config1(cuda, algo, inclusive):
+    # Config 1 (2^20 u32, U[0,15]): the reference's chained scan, this
+    # library (both algorithms) and the oracle agree bit for bit.
     ref = _ref()
     x = rand("u32", 1 << 20, seed=20240601, high=16)
-    want = ref.scan(algo, x, inclusive)
+    want = ref.scan("csdl", x, inclusive)
     assert oracle.validate(x, want, inclusive) == 0  # pins the oracle
     with Plan(algo, "u32", max_n=1 << 20) as plan:
         got = to_host(plan.scan(to_dev(x), inclusive=inclusive), np.uint32)
     assert np.array_equal(got, want)
 
 
+# The reference's SpineScan adds the whole block's total s_red[WARPS - 1]
+# instead of the preceding warps' s_red[WARP_INDEX - 1] for warps >= 1
+# (ReduceThenScan.cuh:91-92), so its reduce-then-scan is exact only while the
+# spine fits in warp 0: up to 129 tiles of 4096, n <= 528384.
+REF_RTS_EXACT_MAX_N = 129 * 4096
+
+
 @pytest.mark.parametrize("inclusive", [False, True])
-def test_reference_rts_agrees_on_wrapping_sums(cuda, inclusive):
+def test_reference_rts_agrees_where_its_spine_is_exact(cuda, inclusive):
     # Full-range values: the reference's reduce-then-scan keeps 32-bit tile
     # sums, so it wraps mod 2^32 exactly like the oracle and this library.
     ref = _ref()
     rng = np.random.default_rng(4)
-    for n in (1, 3, 4095, 4096, 4097, 12289, 100_003, 1 << 20):
+    for n in (1, 3, 4095, 4096, 4097, 12289, 100_003, 300_000, REF_RTS_EXACT_MAX_N):
         x = rng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
         want = ref.scan("rts", x, inclusive)
         assert oracle.validate(x, want, inclusive) == 0, n
         with Plan("rts", "u32", max_n=n) as p1, Plan("csdl", "u32", max_n=n) as p2:
             assert np.array_equal(to_host(p1.scan(to_dev(x), inclusive=inclusive), np.uint32), want)
             assert np.array_equal(to_host(p2.scan(to_dev(x), inclusive=inclusive), np.uint32), want)
+
+
+@pytest.mark.parametrize("inclusive", [False, True])
+def test_reference_rts_spine_defect_beyond_129_tiles(cuda, inclusive):
+    # Config 1 size, 256 tiles: the reference's reduce-then-scan is right on
+    # tiles 0..128 and wrong from tile 129 on; this library's is right
+    # everywhere.
+    ref = _ref()
+    x = rand("u32", 1 << 20, seed=20240601, high=16)
+    want = oracle.scan(x, inclusive)
+    theirs = ref.scan("rts", x, inclusive)
+    with Plan("rts", "u32", max_n=x.size) as plan:
+        ours = to_host(plan.scan(to_dev(x), inclusive=inclusive), np.uint32)
+    assert np.array_equal(ours, want)
+    assert np.array_equal(theirs[:REF_RTS_EXACT_MAX_N], want[:REF_RTS_EXACT_MAX_N])
+    assert not np.array_equal(theirs[REF_RTS_EXACT_MAX_N:], want[REF_RTS_EXACT_MAX_N:])
 
 
 def test_reference_csdl_30_bit_descriptor_limit(cuda):
