@@ -51,7 +51,10 @@ SIGNATURES = [
     ("gps_plan_set_stall", _INT, [_P, _U32, _U32, _U32, _U32, _U32]),
     ("gps_plan_stats", _INT, [_P, _P, ctypes.POINTER(LookbackStats)]),
     ("gps_plan_geometry", _INT, [_P, _U64, ctypes.POINTER(_U32), ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
+    ("gps_scan_u32_noalloc", _INT, [_INT, _P, _P, _U64, _P]),
 ]
+
+NOALLOC_MAX_N = 1 << 28  # GPS_NOALLOC_MAX_N in include/gps.h
 
 
 def load(path: str = LIB_PATH) -> ctypes.CDLL:

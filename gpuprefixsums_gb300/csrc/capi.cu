@@ -107,6 +107,7 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
 
 namespace gps {
 size_t dtype_size(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 8 : 4; }
+void record_error(const char* msg) { g_last_error = msg; }
 }  // namespace gps
 
 extern "C" {

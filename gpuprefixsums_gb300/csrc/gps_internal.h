@@ -108,6 +108,8 @@ cudaError_t launch_rts(gps_dtype dtype, bool inclusive, const ScanArgs& a, void*
                        int num_sms, cudaStream_t stream, LaunchInfo* info);
 
 uint32_t csdl_tile_elems(gps_dtype dtype);
+// Sets the text gps_last_error() returns on this host thread.
+void record_error(const char* msg);
 uint32_t rts_tile_elems(gps_dtype dtype);
 size_t dtype_size(gps_dtype dtype);
 

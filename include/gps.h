@@ -159,6 +159,34 @@ gps_status gps_plan_stats(gps_plan plan, gps_stream_t stream, gps_lookback_stats
 gps_status gps_plan_geometry(gps_plan plan, uint64_t n, uint32_t* tile_elems, uint32_t* grid,
                              uint32_t* launches);
 
+/* Largest n gps_scan_u32_noalloc() accepts: 2^28 elements. */
+#define GPS_NOALLOC_MAX_N (1ull << 28)
+
+/* Chained scan of n uint32 elements that allocates nothing -- for callers
+ * that may not call cudaMalloc (a fixed device-memory budget set by the host
+ * application, a context where the allocator must not be entered, or a
+ * latency-critical path that cannot pay for cudaMalloc's synchronisation).
+ * No counterpart in the reference: its dispatchers always allocate in their
+ * constructors.
+ *
+ * The scratch memory (workspace header and tile descriptors, about 513 KB)
+ * is a fixed array of the library that every GPU which loads the library
+ * holds until the process exits. Same semantics as gps_scan() on a GPS_ALGO_CSDL
+ * / GPS_DTYPE_U32 plan, without a plan: in place or out of place, nothing
+ * written outside [0, n), asynchronous on `stream`. n above
+ * GPS_NOALLOC_MAX_N returns GPS_ERR_SIZE_EXCEEDS_PLAN.
+ *
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current, and sets up the kernels'
+ * launch attributes; make that first call before any stream capture starts.
+ * Every call clears the part of the array it uses with cudaMemsetAsync on
+ * `stream`, because the array keeps what the previous call left. All calls
+ * share the one array: two calls that can run at the same time on the GPU
+ * (different streams, different host threads) race and give wrong results.
+ * Device-side wait timeouts are not reported by this entry point. */
+gps_status gps_scan_u32_noalloc(gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                                gps_stream_t stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
