@@ -37,14 +37,14 @@ cudaError_t launch_csdl_t(const ScanArgs& a, int num_sms, cudaStream_t stream, L
 }
 
 // L2-buffered kernel (16-byte-aligned buffers): 4 reduce + 4 finalize warps
-// over 16 KB tiles, 4 reduce-pass and 8 scan-pass stages (192 KB, one CTA per
+// over 16 KB tiles, 5 reduce-pass and 8 scan-pass stages (208 KB, one CTA per
 // SM), lookback units of 4 tiles (64 KB), 6 units in flight per CTA. The
 // queue depth sets how much input waits in L2 between the two passes
 // (152 x 6 x 64 KB at most): measured on GB300 at 2^28 elements, 6 units
 // beat both 4-5 (too shallow to cover the lookback) and 7-8 (the re-loads
 // start missing in L2).
 constexpr int kL2Warps = 4;
-constexpr int kL2RStages = 4;
+constexpr int kL2RStages = 5;
 constexpr int kL2SStages = 8;
 constexpr int kL2Queue = 6;
 constexpr int kL2Unit = 4;

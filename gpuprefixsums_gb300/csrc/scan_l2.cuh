@@ -6,9 +6,9 @@
 //                L2 evict-last policy, sum it, free the stage at once, and
 //                publish each unit's aggregate (a unit is G tiles taken by
 //                one CTA);
-//   scan pass    once the unit's prefix is known, bulk-load the tile again --
-//                from L2, evict-first -- scan it, add the prefix and
-//                bulk-store it.
+//   scan pass    when the unit's prefix is (about to be) known, bulk-load the
+//                tile again -- from L2, evict-first -- scan it, add the
+//                prefix and bulk-store it.
 // HBM sees one read and one write per element, like the single-pass scan of
 // the reference (ChainedScanDecoupledLookback.cuh:79-139), but the time a tile
 // waits for its lookback is spent in the 129 MB L2 instead of in shared
@@ -17,7 +17,8 @@
 //
 // Warps of a CTA (one CTA per SM):
 //   0          R-loader  takes unit ids (atomic counter), issues reduce-pass loads
-//   1          S-loader  issues scan-pass loads of units whose prefix is known
+//   1          S-loader  issues scan-pass loads of a unit once the previous
+//                        unit's prefix is known
 //   2          storer    bulk-stores scanned tiles, frees scan stages
 //   3..2+LW    lookback  resolve unit prefixes (alternate units), starting as
 //                        soon as a unit id is known
@@ -197,15 +198,19 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                 }
                 const uint32_t u = ctrl->unit_of[q];
                 const bool end = u == kTileEnd;
-                // Load the unit again once its prefix is known (its tiles
-                // were reduced before that, so they are in L2): scan-pass
-                // stages then only hold tiles the finalize warps can finish
-                // at once, and a unit waiting for its lookback waits in L2.
-                if (!end) {
+                // Load the unit again once the previous unit's prefix is
+                // known: its own lookback then usually completes while its
+                // tiles come back from L2 (they were loaded, and reduced, well
+                // before), and the scan-pass stages hold at most one unit
+                // that waits for its prefix; any longer wait is spent in L2.
+                // Entry i - 1 cannot have been reused yet: the finalize warps
+                // still need the tiles of unit i - 1 this thread just issued.
+                if (!end && i >= 1) {
+                    const uint32_t ip = i - 1;
                     bool ready = false;
                     const uint64_t deadline = ptx::global_timer_ns() + long_budget;
-                    while (!(ready = ptx::mbar_try_wait(&ctrl->uprefix[q], ph))) {
-                        if (ld_volatile_u32(&ctrl->end_seq) <= i || ptx::global_timer_ns() > deadline) break;
+                    while (!(ready = ptx::mbar_try_wait(&ctrl->uprefix[ip % Q], (ip / Q) & 1u))) {
+                        if (ld_volatile_u32(&ctrl->end_seq) <= ip || ptx::global_timer_ns() > deadline) break;
                     }
                     if (!ready) {
                         ok = false;
