@@ -21,6 +21,8 @@ GPS_ERR_WRONG_DEVICE = 7
 
 DTYPE_U32 = 0
 DTYPE_U64 = 1
+DTYPE_F32 = 2
+DTYPE_F32_COMPENSATED = 3
 ALGO_CSDL = 0
 ALGO_RTS = 1
 EXCLUSIVE = 0
@@ -46,6 +48,7 @@ SIGNATURES = [
     ("gps_plan_scratch_bytes", _INT, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     ("gps_scan", _INT, [_P, _INT, _P, _P, _U64, _P]),
     ("gps_scan_host", _INT, [_P, _INT, _P, _P, _U64, _P]),
+    ("gps_scan_segmented", _INT, [_P, _INT, _P, _P, _U64, _P, _U64, _P]),
     ("gps_plan_check", _INT, [_P, _P]),
     ("gps_plan_set_wait_budget", _INT, [_P, _U64]),
     ("gps_plan_set_stall", _INT, [_P, _U32, _U32, _U32, _U32, _U32]),

@@ -31,6 +31,7 @@ struct gps_plan_s {
     gps::WsHeader* hdr;
     void* carries;        // two elements (host-array scans)
     void* area;
+    void* desc16;  // 16-byte descriptors of the generic kernel (separate region for u32 plans)
     uint64_t wait_budget_ns;
     gps::StallConfig stall;
     gps::LaunchInfo last_launch;
@@ -63,9 +64,24 @@ constexpr size_t kHeaderBytes = sizeof(gps::WsHeader);
 constexpr size_t kCarryBytes = 128;  // two carry slots, padded to a line
 constexpr uint64_t kDefaultBudgetNs = 1000000000ull;
 
-size_t desc_bytes(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 16 : 8; }
+size_t desc_bytes(gps_dtype dtype) { return dtype == GPS_DTYPE_U32 ? 8 : 16; }
 
-bool valid_dtype(int d) { return d == GPS_DTYPE_U32 || d == GPS_DTYPE_U64; }
+bool valid_dtype(int d) {
+    return d == GPS_DTYPE_U32 || d == GPS_DTYPE_U64 || d == GPS_DTYPE_F32 || d == GPS_DTYPE_F32_COMPENSATED;
+}
+bool is_float(gps_dtype d) { return d == GPS_DTYPE_F32 || d == GPS_DTYPE_F32_COMPENSATED; }
+
+// Generic kernel (scan_seg.cuh): floating-point scans and batched scans.
+cudaError_t launch_generic(gps_dtype dtype, bool inclusive, const gps::ScanArgs& a, const gps::SegArgs* sg,
+                           int num_sms, cudaStream_t stream, gps::LaunchInfo* info) {
+    switch (dtype) {
+        case GPS_DTYPE_U32: return gps::launch_seg_u32(inclusive, a, sg, num_sms, stream, info);
+        case GPS_DTYPE_U64: return gps::launch_seg_u64(inclusive, a, sg, num_sms, stream, info);
+        case GPS_DTYPE_F32: return gps::launch_seg_f32(inclusive, a, sg, num_sms, stream, info);
+        case GPS_DTYPE_F32_COMPENSATED: return gps::launch_seg_f32c(inclusive, a, sg, num_sms, stream, info);
+    }
+    return cudaErrorInvalidValue;
+}
 bool valid_algo(int a) { return a == GPS_ALGO_CSDL || a == GPS_ALGO_RTS; }
 bool valid_kind(int k) { return k == GPS_SCAN_EXCLUSIVE || k == GPS_SCAN_INCLUSIVE; }
 
@@ -94,7 +110,10 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     a.wait_budget_ns = p->wait_budget_ns;
     a.stall = p->stall;
     cudaError_t err;
-    if (p->algo == GPS_ALGO_CSDL) {
+    if (is_float(p->dtype)) {
+        a.desc = p->desc16;
+        err = launch_generic(p->dtype, inclusive, a, nullptr, p->num_sms, stream, &p->last_launch);
+    } else if (p->algo == GPS_ALGO_CSDL) {
         err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0, a, p->num_sms, stream, &p->last_launch);
     } else {
         err = gps::launch_rts(p->dtype, inclusive, a, p->area, p->num_sms, stream, &p->last_launch);
@@ -136,6 +155,8 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     if (!valid_algo(algo)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown algorithm %d", static_cast<int>(algo));
     if (!valid_dtype(dtype)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown dtype %d", static_cast<int>(dtype));
     if (max_n == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "max_n must be at least 1");
+    if (is_float(dtype) && algo != GPS_ALGO_CSDL)
+        return fail(GPS_ERR_UNSUPPORTED, "floating-point scans use the chained scan (GPS_ALGO_CSDL)");
     const uint32_t tile = algo == GPS_ALGO_CSDL ? gps::csdl_tile_elems(dtype) : gps::rts_tile_elems(dtype);
     const uint64_t tiles = (max_n + tile - 1) / tile;
     if (tiles >= (1ull << 31))
@@ -160,7 +181,11 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     // reduce-then-scan: one tile sum per tile.
     const size_t per_tile = algo == GPS_ALGO_CSDL ? desc_bytes(dtype) : gps::dtype_size(dtype);
     const uint64_t slots = algo == GPS_ALGO_CSDL ? tiles + gps::kDescPad : tiles;
-    p->scratch_bytes = kHeaderBytes + kCarryBytes + slots * per_tile;
+    // u32 chained-scan plans keep 8-byte descriptors; batched scans of them
+    // use the generic kernel's 16-byte descriptors, kept in a region of their
+    // own so that the two formats never meet in one slot.
+    const uint64_t slots16 = (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? tiles + gps::kDescPad : 0;
+    p->scratch_bytes = kHeaderBytes + kCarryBytes + slots * per_tile + slots16 * 16;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;
@@ -170,6 +195,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->hdr = static_cast<gps::WsHeader*>(p->scratch);
     p->carries = static_cast<char*>(p->scratch) + kHeaderBytes;
     p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
+    p->desc16 = slots16 ? static_cast<char*>(p->area) + slots * per_tile : p->area;
     gps::WsHeader h{};
     h.epoch = 1;
     h.capacity_tiles = slots;
@@ -229,10 +255,53 @@ gps_status gps_scan(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_ou
     const uint64_t bytes = n * es;
     if (i != o && i < o + bytes && o < i + bytes)
         return fail(GPS_ERR_INVALID_ARGUMENT, "input and output overlap without being identical");
+    if (is_float(p->dtype) && ((i | o) & 15u) != 0)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "floating-point scans need 16-byte aligned buffers");
     gps_status st = check_device(p);
     if (st != GPS_OK) return st;
     return launch_scan(p, kind == GPS_SCAN_INCLUSIVE, d_in, d_out, n, nullptr, nullptr,
                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+gps_status gps_scan_segmented(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                              const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
+    if (p->algo != GPS_ALGO_CSDL)
+        return fail(GPS_ERR_UNSUPPORTED, "batched scans run on chained-scan plans (GPS_ALGO_CSDL)");
+    if (n == 0) return GPS_OK;
+    if (num_segments == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "%llu elements but no segments",
+                                       static_cast<unsigned long long>(n));
+    if (n > p->max_n)
+        return fail(GPS_ERR_SIZE_EXCEEDS_PLAN, "requested size %llu exceeds the plan's maximum %llu",
+                    static_cast<unsigned long long>(n), static_cast<unsigned long long>(p->max_n));
+    if (n > 0xFFFFFFFFull || num_segments > 0xFFFFFFFEull)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "uint32 offsets limit a batch to 2^32 - 1 elements");
+    if (d_in == nullptr || d_out == nullptr || d_offsets == nullptr)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "NULL pointer");
+    const size_t es = gps::dtype_size(p->dtype);
+    const uintptr_t i = reinterpret_cast<uintptr_t>(d_in), o = reinterpret_cast<uintptr_t>(d_out);
+    if (((i | o) & 15u) != 0) return fail(GPS_ERR_INVALID_ARGUMENT, "batched scans need 16-byte aligned buffers");
+    if ((reinterpret_cast<uintptr_t>(d_offsets) & 3u) != 0)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "offsets must be 4-byte aligned");
+    const uint64_t bytes = n * es;
+    if (i != o && i < o + bytes && o < i + bytes)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "input and output overlap without being identical");
+    gps_status st = check_device(p);
+    if (st != GPS_OK) return st;
+    gps::ScanArgs a{};
+    a.in = d_in;
+    a.out = d_out;
+    a.n = n;
+    a.num_tiles = static_cast<uint32_t>((n + p->tile_elems - 1) / p->tile_elems);
+    a.hdr = p->hdr;
+    a.desc = p->desc16;
+    a.wait_budget_ns = p->wait_budget_ns;
+    const gps::SegArgs sg{d_offsets, static_cast<uint32_t>(num_segments)};
+    const cudaError_t err = launch_generic(p->dtype, kind == GPS_SCAN_INCLUSIVE, a, &sg, p->num_sms,
+                                           reinterpret_cast<cudaStream_t>(stream), &p->last_launch);
+    if (err != cudaSuccess) return cuda_fail(err, "batched scan launch");
+    return GPS_OK;
 }
 
 gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void* h_out, uint64_t n,
@@ -241,6 +310,7 @@ gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void*
     if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
     if (n == 0) return GPS_OK;
     if (h_in == nullptr || h_out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL data pointer");
+    if (is_float(p->dtype)) return fail(GPS_ERR_UNSUPPORTED, "host-array scans are integer only");
     gps_status st = check_device(p);
     if (st != GPS_OK) return st;
     const size_t es = gps::dtype_size(p->dtype);

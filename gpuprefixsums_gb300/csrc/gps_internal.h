@@ -94,6 +94,13 @@ struct TileShape {
     static constexpr int kThreads = 32 * (1 + kLookbackWarps + 2 * RW);
 };
 
+// Segments of a batched (segmented) scan: segment s is
+// [offsets[s], offsets[s+1]); offsets has num_segments + 1 entries.
+struct SegArgs {
+    const uint32_t* offsets;
+    uint32_t num_segments;
+};
+
 // ------------------------------------------------------------ launchers
 // Each returns the launch status; they never synchronize.
 struct LaunchInfo {
@@ -106,6 +113,16 @@ cudaError_t launch_csdl(gps_dtype dtype, bool inclusive, bool stall_mode, const 
                         int num_sms, cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_rts(gps_dtype dtype, bool inclusive, const ScanArgs& a, void* tile_sums,
                        int num_sms, cudaStream_t stream, LaunchInfo* info);
+// Generic single-pass scan (scan_seg.cuh), one per scan operation; `sg` null
+// for a plain scan. Buffers must be 16-byte aligned; descriptors are 16 bytes.
+cudaError_t launch_seg_u32(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
+                           LaunchInfo* info);
+cudaError_t launch_seg_u64(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
+                           LaunchInfo* info);
+cudaError_t launch_seg_f32(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
+                           LaunchInfo* info);
+cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
+                            LaunchInfo* info);
 
 uint32_t csdl_tile_elems(gps_dtype dtype);
 // Sets the text gps_last_error() returns on this host thread.

@@ -1,0 +1,126 @@
+// Scan operations for the generic single-pass kernel (scan_seg.cuh).
+//
+// Each operation fixes
+//   T  element type in memory,
+//   S  running state inside a CTA (the element type, or a double-float pair
+//      for the compensated FP32 scan),
+//   C  value carried between lookback units in the tile descriptors (the
+//      element type, or FP64 for the compensated FP32 scan),
+// and the associative combine of S and of C. Integer scans wrap mod 2^w.
+#pragma once
+#include <cstdint>
+
+namespace gps {
+
+template <typename S>
+__device__ __forceinline__ S shfl_any(S s, uint32_t src);
+template <typename S>
+__device__ __forceinline__ S shfl_up_any(S s, uint32_t d);
+
+template <>
+__device__ __forceinline__ uint32_t shfl_any(uint32_t s, uint32_t src) { return __shfl_sync(0xFFFFFFFFu, s, src); }
+template <>
+__device__ __forceinline__ uint64_t shfl_any(uint64_t s, uint32_t src) { return __shfl_sync(0xFFFFFFFFu, s, src); }
+template <>
+__device__ __forceinline__ float shfl_any(float s, uint32_t src) { return __shfl_sync(0xFFFFFFFFu, s, src); }
+template <>
+__device__ __forceinline__ double shfl_any(double s, uint32_t src) { return __shfl_sync(0xFFFFFFFFu, s, src); }
+template <>
+__device__ __forceinline__ uint32_t shfl_up_any(uint32_t s, uint32_t d) { return __shfl_up_sync(0xFFFFFFFFu, s, d); }
+template <>
+__device__ __forceinline__ uint64_t shfl_up_any(uint64_t s, uint32_t d) { return __shfl_up_sync(0xFFFFFFFFu, s, d); }
+template <>
+__device__ __forceinline__ float shfl_up_any(float s, uint32_t d) { return __shfl_up_sync(0xFFFFFFFFu, s, d); }
+
+// ------------------------------------------------------------- integers
+template <typename U>
+struct OpInt {
+    using T = U;
+    using S = U;
+    using C = U;
+    __device__ static S zero() { return 0; }
+    __device__ static S lift(T x) { return x; }
+    __device__ static S add(S a, S b) { return a + b; }
+    __device__ static T out(S s) { return s; }
+    __device__ static C to_chain(S s) { return s; }
+    __device__ static S from_chain(C c) { return c; }
+    __device__ static C chain_zero() { return 0; }
+    __device__ static C chain_add(C a, C b) { return a + b; }
+    __device__ static uint64_t chain_bits(C c) { return static_cast<uint64_t>(c); }
+    __device__ static C chain_from_bits(uint64_t b) { return static_cast<C>(b); }
+    __device__ static S shfl(S s, uint32_t src) { return shfl_any(s, src); }
+    __device__ static S shfl_up(S s, uint32_t d) { return shfl_up_any(s, d); }
+    __device__ static C chain_shfl_xor(C c, uint32_t m) { return __shfl_xor_sync(0xFFFFFFFFu, c, m); }
+};
+using OpU32 = OpInt<uint32_t>;
+using OpU64 = OpInt<uint64_t>;
+
+// ------------------------------------------------------------ plain FP32
+// Left-to-right float additions inside a thread, float shuffle and block
+// trees, float carried between units: the uncompensated baseline.
+struct OpF32 {
+    using T = float;
+    using S = float;
+    using C = float;
+    __device__ static S zero() { return 0.0f; }
+    __device__ static S lift(T x) { return x; }
+    __device__ static S add(S a, S b) { return a + b; }
+    __device__ static T out(S s) { return s; }
+    __device__ static C to_chain(S s) { return s; }
+    __device__ static S from_chain(C c) { return c; }
+    __device__ static C chain_zero() { return 0.0f; }
+    __device__ static C chain_add(C a, C b) { return a + b; }
+    __device__ static uint64_t chain_bits(C c) { return __float_as_uint(c); }
+    __device__ static C chain_from_bits(uint64_t b) { return __uint_as_float(static_cast<uint32_t>(b)); }
+    __device__ static S shfl(S s, uint32_t src) { return shfl_any(s, src); }
+    __device__ static S shfl_up(S s, uint32_t d) { return shfl_up_any(s, d); }
+    __device__ static C chain_shfl_xor(C c, uint32_t m) { return __shfl_xor_sync(0xFFFFFFFFu, c, m); }
+};
+
+// ------------------------------------------------------ compensated FP32
+// Double-float state: hi carries the rounded sum, lo the rounding error of
+// everything added so far. Every add is Knuth's TwoSum on the high parts
+// (exact for operands of any magnitude order), the low parts are added to
+// the error, and Fast2Sum renormalises the pair (Dekker 1971; Knuth, TAOCP
+// vol. 2, 4.2.2). Bulk arithmetic stays in FP32; only the value carried from
+// one lookback unit to the next is FP64.
+struct F2 {
+    float hi, lo;
+};
+
+struct OpF32C {
+    using T = float;
+    using S = F2;
+    using C = double;
+    __device__ static S zero() { return F2{0.0f, 0.0f}; }
+    __device__ static S lift(T x) { return F2{x, 0.0f}; }
+    __device__ static S add(S a, S b) {
+        const float s = a.hi + b.hi;
+        const float bb = s - a.hi;
+        float e = (a.hi - (s - bb)) + (b.hi - bb);
+        e += a.lo + b.lo;
+        const float hi = s + e;
+        const float lo = e - (hi - s);
+        return F2{hi, lo};
+    }
+    __device__ static T out(S s) { return s.hi + s.lo; }
+    __device__ static C to_chain(S s) { return static_cast<double>(s.hi) + static_cast<double>(s.lo); }
+    __device__ static S from_chain(C c) {
+        const float hi = static_cast<float>(c);
+        const float lo = static_cast<float>(c - static_cast<double>(hi));
+        return F2{hi, lo};
+    }
+    __device__ static C chain_zero() { return 0.0; }
+    __device__ static C chain_add(C a, C b) { return a + b; }
+    __device__ static uint64_t chain_bits(C c) { return static_cast<uint64_t>(__double_as_longlong(c)); }
+    __device__ static C chain_from_bits(uint64_t b) { return __longlong_as_double(static_cast<long long>(b)); }
+    __device__ static S shfl(S s, uint32_t src) {
+        return F2{__shfl_sync(0xFFFFFFFFu, s.hi, src), __shfl_sync(0xFFFFFFFFu, s.lo, src)};
+    }
+    __device__ static S shfl_up(S s, uint32_t d) {
+        return F2{__shfl_up_sync(0xFFFFFFFFu, s.hi, d), __shfl_up_sync(0xFFFFFFFFu, s.lo, d)};
+    }
+    __device__ static C chain_shfl_xor(C c, uint32_t m) { return __shfl_xor_sync(0xFFFFFFFFu, c, m); }
+};
+
+}  // namespace gps

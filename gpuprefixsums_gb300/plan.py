@@ -14,7 +14,8 @@ from . import _lib
 from ._lib import check, lib
 
 _ALGOS = {"csdl": _lib.ALGO_CSDL, "rts": _lib.ALGO_RTS}
-_DTYPES = {"u32": (_lib.DTYPE_U32, 4), "u64": (_lib.DTYPE_U64, 8)}
+_DTYPES = {"u32": (_lib.DTYPE_U32, 4), "u64": (_lib.DTYPE_U64, 8), "f32": (_lib.DTYPE_F32, 4),
+           "f32c": (_lib.DTYPE_F32_COMPENSATED, 4)}
 
 
 def _stream_handle(stream) -> int:
@@ -82,6 +83,23 @@ class Plan:
         if count > x.numel() or count > out.numel():
             raise ValueError("n exceeds the tensor length")
         self.scan_ptr(x.data_ptr(), out.data_ptr(), count, inclusive, stream)
+        return out
+
+    def scan_segmented(self, x, offsets, out=None, inclusive: bool = False, stream=None):
+        """Batched scan: independent scans of the segments [offsets[s],
+        offsets[s+1]) of CUDA tensor x (offsets: int32/uint32 CUDA tensor of
+        num_segments + 1 entries, offsets[0] == 0, offsets[-1] == x.numel())."""
+        if x.element_size() != self.elem_size or not (x.is_cuda and x.is_contiguous()):
+            raise ValueError("x must be a contiguous CUDA tensor with the plan's element size")
+        if offsets.element_size() != 4 or not (offsets.is_cuda and offsets.is_contiguous()):
+            raise ValueError("offsets must be a contiguous 32-bit CUDA tensor")
+        if out is None:
+            import torch
+            out = torch.empty_like(x)
+        kind = _lib.INCLUSIVE if inclusive else _lib.EXCLUSIVE
+        check(lib.gps_scan_segmented(self._h, kind, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                     x.numel(), ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1,
+                                     ctypes.c_void_p(_stream_handle(stream))), "gps_scan_segmented")
         return out
 
     def scan_host(self, h_in: int, h_out: int, n: int, inclusive: bool = False, stream=None) -> None:

@@ -54,7 +54,13 @@ typedef enum gps_status {
 
 typedef enum gps_dtype {
     GPS_DTYPE_U32 = 0, /* uint32_t, sums wrap mod 2^32 (the reference's type) */
-    GPS_DTYPE_U64 = 1  /* uint64_t, sums wrap mod 2^64 */
+    GPS_DTYPE_U64 = 1, /* uint64_t, sums wrap mod 2^64 */
+    /* float, plain FP32 arithmetic throughout (GPS_ALGO_CSDL only) */
+    GPS_DTYPE_F32 = 2,
+    /* float in and out; each partial sum carries a TwoSum error term through
+     * the thread, warp and block scans, and the value passed between lookback
+     * units is FP64 (GPS_ALGO_CSDL only) */
+    GPS_DTYPE_F32_COMPENSATED = 3
 } gps_dtype;
 
 typedef enum gps_algo {
@@ -110,6 +116,18 @@ gps_status gps_plan_scratch_bytes(gps_plan plan, size_t* out_bytes);
  * buffer in place. */
 gps_status gps_scan(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
                     gps_stream_t stream);
+
+/* Batched scan: num_segments independent scans of the segments
+ * [d_offsets[s], d_offsets[s+1]) of d_in (CSR offsets, uint32, num_segments + 1
+ * entries, d_offsets[0] == 0 and d_offsets[num_segments] == n), in ONE launch:
+ * each segment's output restarts at its first element (0 for an exclusive
+ * scan). Empty segments are allowed. Any dtype on a GPS_ALGO_CSDL plan;
+ * 16-byte aligned d_in and d_out; n <= 2^32 - 1; in place or out of place.
+ * Asynchronous on `stream`, and capturable in a CUDA graph.
+ * No counterpart in the reference: it scans one buffer per dispatch; this
+ * replaces a loop of DispatchKernels{Ex,In}clusive calls, one per segment. */
+gps_status gps_scan_segmented(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                              const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream);
 
 /* Scan of a host array: copies h_in to the device, scans, copies the result
  * to h_out, in chunks so that the copies in both directions overlap the

@@ -1,0 +1,175 @@
+"""Batched (segmented) scans and floating-point scans on the GPU, through the
+C ABI, against the oracle.
+
+Integer results are bit-exact (segmented oracle: oracle.segscan). Floating-
+point results are compared with the exact prefix sums of the FP32 inputs
+(oracle.scan_f32_exact: fixed-point superaccumulator, rounded once to FP64):
+- compensated FP32: relative error of every nonzero prefix <= 1e-6 and the
+  error relative to the sum of magnitudes so far (normwise) <= 1e-7 (rounding
+  the exact prefix to FP32 alone costs up to 2^-24 = 6e-8 of either);
+- plain FP32: normwise error <= 1e-5 (FP32 sums of up to 2^26 terms).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gpuprefixsums_gb300 import Plan
+
+pytestmark = pytest.mark.gpu
+
+NP = {"u32": np.uint32, "u64": np.uint64}
+TV = {"u32": np.int32, "u64": np.int64}
+
+
+def dev(x):
+    v = {np.dtype(np.uint32): np.int32, np.dtype(np.uint64): np.int64}.get(x.dtype, None)
+    return torch.from_numpy(np.ascontiguousarray(x).view(v) if v else np.ascontiguousarray(x)).cuda()
+
+
+def offsets_of(lengths):
+    return np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint64)
+
+
+def config3_lengths(seed=3):
+    # 4096 segments, lengths floor(log-uniform[1, 2^20]).
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(0.0, np.log(2.0 ** 20), size=4096))).astype(np.int64)
+
+
+@pytest.mark.parametrize("dtype", ["u32", "u64"])
+@pytest.mark.parametrize("inclusive", [False, True])
+def test_segmented_random_lengths_bit_exact(cuda, dtype, inclusive):
+    rng = np.random.default_rng(17)
+    # Many short segments, empty ones, and some spanning several units.
+    lengths = np.concatenate([rng.integers(0, 40, size=3000), rng.integers(0, 5000, size=300),
+                              rng.integers(10_000, 300_000, size=12), [0, 0, 1, 1, 0]])
+    rng.shuffle(lengths)
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    x = rng.integers(0, np.iinfo(NP[dtype]).max, size=n, dtype=NP[dtype], endpoint=True)
+    want = oracle.segscan(x, offs, inclusive)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    with Plan("csdl", dtype, max_n=n) as plan:
+        got = plan.scan_segmented(dev(x), d_off, inclusive=inclusive)
+        plan.check()
+    assert np.array_equal(got.cpu().numpy().view(NP[dtype]), want)
+
+
+def test_segmented_config3_4096_segments_in_place(cuda):
+    lengths = config3_lengths()
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    rng = np.random.default_rng(30)
+    x = rng.integers(0, 256, size=n, dtype=np.uint32)
+    want = oracle.segscan(x, offs, False)
+    d = dev(x)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    with Plan("csdl", "u32", max_n=n) as plan:
+        plan.scan_segmented(d, d_off, out=d, inclusive=False)
+        plan.check()
+    assert np.array_equal(d.cpu().numpy().view(np.uint32), want)
+
+
+def test_segmented_equals_looped_plain_scans_and_replays_from_a_graph(cuda):
+    lengths = config3_lengths(seed=5)[:300]
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    rng = np.random.default_rng(31)
+    x = rng.integers(0, 256, size=n, dtype=np.uint32)
+    d_in = dev(x)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    looped = torch.empty_like(d_in)
+    with Plan("csdl", "u32", max_n=n) as plan:
+        for s in range(len(lengths)):
+            b, e = int(offs[s]), int(offs[s + 1])
+            if e > b:
+                plan.scan(d_in[b:e], looped[b:e], inclusive=False)
+        batched = plan.scan_segmented(d_in, d_off)
+        torch.cuda.synchronize()
+        assert torch.equal(batched, looped)
+        g = torch.cuda.CUDAGraph()
+        st = torch.cuda.Stream()
+        out = torch.empty_like(d_in)
+        with torch.cuda.stream(st):
+            with torch.cuda.graph(g, stream=st):
+                plan.scan_segmented(d_in, d_off, out=out, stream=st)
+        for _ in range(5):
+            out.zero_()
+            g.replay()
+            torch.cuda.synchronize()
+            assert torch.equal(out, looped)
+        plan.check()
+
+
+# ------------------------------------------------------------ floating point
+def fp_errors(got, exact, x):
+    got = got.astype(np.float64)
+    nz = exact != 0
+    rel = np.abs(got[nz] - exact[nz]) / np.abs(exact[nz])
+    if rel.size == 0:  # every exact prefix is zero (e.g. an exclusive scan of one element)
+        rel = np.abs(got)
+    mag = np.cumsum(np.abs(x.astype(np.float64)))
+    norm = np.abs(got - exact) / np.maximum(mag, np.finfo(np.float64).tiny)
+    return float(rel.max()), float(np.median(rel)), float(norm.max())
+
+
+def fp_input(kind, n, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "normal":
+        return rng.standard_normal(n).astype(np.float32)
+    mag = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), size=n))
+    return (mag * rng.choice([-1.0, 1.0], size=n)).astype(np.float32)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("kind", ["normal", "mixed"])
+def test_config4_fp32_2pow26_plain_and_compensated(cuda, kind):
+    n = 1 << 26
+    x = fp_input(kind, n, seed=26 if kind == "normal" else 27)
+    exact = oracle.scan_f32_exact(x, inclusive=True)
+    d = torch.from_numpy(x).cuda()
+    res = {}
+    for dt in ("f32", "f32c"):
+        with Plan("csdl", dt, max_n=n) as plan:
+            res[dt] = fp_errors(plan.scan(d, inclusive=True).cpu().numpy(), exact, x)
+            plan.check()
+    rel_c, med_c, norm_c = res["f32c"]
+    print(kind, res)
+    assert rel_c <= 1e-6 and norm_c <= 1e-7, res
+    assert res["f32"][2] <= 1e-5, res
+    assert res["f32"][0] > rel_c, res
+
+
+@pytest.mark.parametrize("dt", ["f32", "f32c"])
+@pytest.mark.parametrize("inclusive", [False, True])
+def test_fp32_sizes_and_segments(cuda, dt, inclusive):
+    rng = np.random.default_rng(4)
+    for n in (1, 5, 4096, 4097, 16384 * 3 + 11, 1_000_003):
+        x = fp_input("normal", n, seed=n)
+        exact = oracle.scan_f32_exact(x, inclusive=inclusive)
+        with Plan("csdl", dt, max_n=n) as plan:
+            got = plan.scan(torch.from_numpy(x).cuda(), inclusive=inclusive).cpu().numpy()
+            plan.check()
+        rel, _, norm = fp_errors(got, exact, x)
+        if dt == "f32c":
+            assert rel <= 1e-6, (n, rel)
+        else:
+            assert norm <= 1e-5, (n, norm)
+    # segmented, compared segment by segment with the exact prefix sums
+    lengths = np.concatenate([rng.integers(0, 50, size=500), rng.integers(1000, 70_000, size=10)])
+    rng.shuffle(lengths)
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    x = fp_input("mixed", n, seed=99)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    with Plan("csdl", dt, max_n=n) as plan:
+        got = plan.scan_segmented(torch.from_numpy(x).cuda(), d_off, inclusive=inclusive).cpu().numpy()
+        plan.check()
+    worst = 0.0
+    for s in range(len(lengths)):
+        b, e = int(offs[s]), int(offs[s + 1])
+        if e > b:
+            ex = oracle.scan_f32_exact(x[b:e], inclusive=inclusive)
+            worst = max(worst, fp_errors(got[b:e], ex, x[b:e])[2])
+    assert worst <= (1e-7 if dt == "f32c" else 1e-5), worst
