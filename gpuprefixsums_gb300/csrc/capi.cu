@@ -31,7 +31,12 @@ struct gps_plan_s {
     gps::WsHeader* hdr;
     void* carries;        // two elements (host-array scans)
     void* area;
-    void* desc16;  // 16-byte descriptors of the generic kernel (separate region for u32 plans)
+    // Generic kernel (batched and floating-point scans): its workspace header
+    // and 16-byte descriptors. On u32 chained-scan plans they are a region of
+    // their own, with their own epoch, next to the 8-byte descriptors of the
+    // u32 kernel; on other plans they are hdr and area.
+    gps::WsHeader* hdr16;
+    void* desc16;
     uint64_t wait_budget_ns;
     gps::StallConfig stall;
     gps::LaunchInfo last_launch;
@@ -111,6 +116,7 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     a.stall = p->stall;
     cudaError_t err;
     if (is_float(p->dtype)) {
+        a.hdr = p->hdr16;
         a.desc = p->desc16;
         err = launch_generic(p->dtype, inclusive, a, nullptr, p->num_sms, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
@@ -185,7 +191,11 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     // use the generic kernel's 16-byte descriptors, kept in a region of their
     // own so that the two formats never meet in one slot.
     const uint64_t slots16 = (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? tiles + gps::kDescPad : 0;
-    p->scratch_bytes = kHeaderBytes + kCarryBytes + slots * per_tile + slots16 * 16;
+    // [header][carries][descriptors or tile sums] and, for u32 chained-scan
+    // plans, [256-byte aligned: generic header][16-byte descriptors].
+    const size_t main_bytes = kHeaderBytes + kCarryBytes + slots * per_tile;
+    const size_t region16 = (main_bytes + 255) & ~static_cast<size_t>(255);
+    p->scratch_bytes = slots16 ? region16 + kHeaderBytes + slots16 * 16 : main_bytes;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;
@@ -195,12 +205,17 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->hdr = static_cast<gps::WsHeader*>(p->scratch);
     p->carries = static_cast<char*>(p->scratch) + kHeaderBytes;
     p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
-    p->desc16 = slots16 ? static_cast<char*>(p->area) + slots * per_tile : p->area;
+    p->hdr16 = slots16 ? reinterpret_cast<gps::WsHeader*>(static_cast<char*>(p->scratch) + region16) : p->hdr;
+    p->desc16 = slots16 ? static_cast<char*>(p->scratch) + region16 + kHeaderBytes : p->area;
     gps::WsHeader h{};
     h.epoch = 1;
     h.capacity_tiles = slots;
     err = cudaMemset(p->scratch, 0, p->scratch_bytes);
     if (err == cudaSuccess) err = cudaMemcpy(p->hdr, &h, sizeof(h), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && slots16) {
+        h.capacity_tiles = slots16;
+        err = cudaMemcpy(p->hdr16, &h, sizeof(h), cudaMemcpyHostToDevice);
+    }
     if (err == cudaSuccess) err = cudaDeviceSynchronize();
     if (err != cudaSuccess) {
         cudaFree(p->scratch);
@@ -294,9 +309,11 @@ gps_status gps_scan_segmented(gps_plan p, gps_scan_kind kind, const void* d_in, 
     a.out = d_out;
     a.n = n;
     a.num_tiles = static_cast<uint32_t>((n + p->tile_elems - 1) / p->tile_elems);
-    a.hdr = p->hdr;
+    a.hdr = p->hdr16;
     a.desc = p->desc16;
     a.wait_budget_ns = p->wait_budget_ns;
+    if ((reinterpret_cast<uintptr_t>(p->desc16) & 15u) != 0)
+        return fail(GPS_ERR_CUDA, "internal: misaligned descriptor region");
     const gps::SegArgs sg{d_offsets, static_cast<uint32_t>(num_segments)};
     const cudaError_t err = launch_generic(p->dtype, kind == GPS_SCAN_INCLUSIVE, a, &sg, p->num_sms,
                                            reinterpret_cast<cudaStream_t>(stream), &p->last_launch);
@@ -373,15 +390,20 @@ gps_status gps_plan_check(gps_plan p, gps_stream_t stream) {
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     cudaError_t err = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
     if (err != cudaSuccess) return cuda_fail(err, "cudaStreamSynchronize");
-    uint32_t flags = 0;
-    err = cudaMemcpy(&flags, &p->hdr->error_flags, sizeof(flags), cudaMemcpyDeviceToHost);
-    if (err != cudaSuccess) return cuda_fail(err, "reading device error flags");
-    if (flags != 0) {
-        const uint32_t zero = 0;
-        err = cudaMemcpy(&p->hdr->error_flags, &zero, sizeof(zero), cudaMemcpyHostToDevice);
-        if (err != cudaSuccess) return cuda_fail(err, "clearing device error flags");
-        return fail(GPS_ERR_TIMEOUT, "a device-side wait exceeded its budget (flags 0x%x)", flags);
+    uint32_t all = 0;
+    for (gps::WsHeader* h : {p->hdr, p->hdr16}) {
+        if (h == p->hdr16 && h == p->hdr) break;
+        uint32_t flags = 0;
+        err = cudaMemcpy(&flags, &h->error_flags, sizeof(flags), cudaMemcpyDeviceToHost);
+        if (err != cudaSuccess) return cuda_fail(err, "reading device error flags");
+        if (flags != 0) {
+            const uint32_t zero = 0;
+            err = cudaMemcpy(&h->error_flags, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+            if (err != cudaSuccess) return cuda_fail(err, "clearing device error flags");
+        }
+        all |= flags;
     }
+    if (all != 0) return fail(GPS_ERR_TIMEOUT, "a device-side wait exceeded its budget (flags 0x%x)", all);
     return GPS_OK;
 }
 

@@ -41,6 +41,9 @@ struct OpInt {
     __device__ static S zero() { return 0; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
+    __device__ static S acc(S a, T x) { return a + x; }
+    __device__ static S combine(S a, S b) { return a + b; }
+    __device__ static S norm(S a) { return a; }
     __device__ static T out(S s) { return s; }
     __device__ static C to_chain(S s) { return s; }
     __device__ static S from_chain(C c) { return c; }
@@ -65,6 +68,9 @@ struct OpF32 {
     __device__ static S zero() { return 0.0f; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
+    __device__ static S acc(S a, T x) { return a + x; }
+    __device__ static S combine(S a, S b) { return a + b; }
+    __device__ static S norm(S a) { return a; }
     __device__ static T out(S s) { return s; }
     __device__ static C to_chain(S s) { return s; }
     __device__ static S from_chain(C c) { return c; }
@@ -79,11 +85,17 @@ struct OpF32 {
 
 // ------------------------------------------------------ compensated FP32
 // Double-float state: hi carries the rounded sum, lo the rounding error of
-// everything added so far. Every add is Knuth's TwoSum on the high parts
-// (exact for operands of any magnitude order), the low parts are added to
-// the error, and Fast2Sum renormalises the pair (Dekker 1971; Knuth, TAOCP
-// vol. 2, 4.2.2). Bulk arithmetic stays in FP32; only the value carried from
-// one lookback unit to the next is FP64.
+// everything added so far. Combining two states is Knuth's TwoSum on the high
+// parts (exact for operands of any magnitude order), the low parts are added
+// to the error, and Fast2Sum renormalises the pair (Dekker 1971; Knuth, TAOCP
+// vol. 2, 4.2.2). Adding one input to a state (acc) is TwoSum without the
+// renormalisation: the only dependency from one item to the next is then a
+// single FP32 add on hi and one on lo, and norm() renormalises with TwoSum
+// once per thread. combine() merges two states the same lazy way (used by
+// the warp, block and chunk scans, whose chains are then one FP32 add deep per
+// step); lo stays within a few units in the last place of hi, and hi + lo is
+// exact in FP64 and rounds once to the FP32 output. Bulk arithmetic stays in
+// FP32; only the value carried from one lookback unit to the next is FP64.
 struct F2 {
     float hi, lo;
 };
@@ -102,6 +114,23 @@ struct OpF32C {
         const float hi = s + e;
         const float lo = e - (hi - s);
         return F2{hi, lo};
+    }
+    __device__ static S acc(S a, T x) {
+        const float s = a.hi + x;
+        const float bb = s - a.hi;
+        const float e = (a.hi - (s - bb)) + (x - bb);
+        return F2{s, a.lo + e};
+    }
+    __device__ static S combine(S a, S b) {
+        const float s = a.hi + b.hi;
+        const float bb = s - a.hi;
+        const float e = (a.hi - (s - bb)) + (b.hi - bb);
+        return F2{s, a.lo + (b.lo + e)};
+    }
+    __device__ static S norm(S a) {
+        const float s = a.hi + a.lo;
+        const float bb = s - a.hi;
+        return F2{s, (a.hi - (s - bb)) + (a.lo - bb)};
     }
     __device__ static T out(S s) { return s.hi + s.lo; }
     __device__ static C to_chain(S s) { return static_cast<double>(s.hi) + static_cast<double>(s.lo); }

@@ -58,7 +58,7 @@ __device__ __forceinline__ void rotate_chunks(T (&v)[CHUNKS * EPC], uint32_t amo
 // Segmented combine of (a, fa) followed by (b, fb).
 template <class Op>
 __device__ __forceinline__ void seg_combine(typename Op::S& a, bool& fa, typename Op::S b, bool fb) {
-    a = fb ? b : Op::add(a, b);
+    a = fb ? b : Op::combine(a, b);
     fa = fa || fb;
 }
 
@@ -67,6 +67,61 @@ __device__ __forceinline__ typename Op::C chain_warp_sum(typename Op::C x) {
 #pragma unroll
     for (int m = 16; m; m >>= 1) x = Op::chain_add(x, Op::chain_shfl_xor(x, m));
     return x;
+}
+
+// Per-thread work on a thread's CHUNKS x EPC items. Register chunk c holds
+// logical chunk (c + rrot) & (CHUNKS - 1) (the bank-conflict-free read order;
+// rrot = 0 when the items were read in logical order). hb holds the items'
+// head bits in logical order. Each chunk is summed by its own chain of EPC
+// items, so a thread runs CHUNKS short independent chains instead of one long
+// one; only the CHUNKS chunk aggregates are then put in logical order.
+template <class Op, int CHUNKS, int EPC, bool SEG>
+__device__ __forceinline__ uint32_t chunk_head_bits(uint32_t hb, uint32_t c, uint32_t rrot) {
+    if (!SEG) return 0u;
+    const uint32_t l = (c + rrot) & (CHUNKS - 1);
+    return (hb >> (l * EPC)) & ((1u << EPC) - 1u);
+}
+
+// Chunk aggregates in logical order; returns the mask (logical order) of the
+// chunks that hold a segment head.
+template <class Op, int CHUNKS, int EPC, bool SEG, bool REORDER>
+__device__ __forceinline__ uint32_t chunk_aggregates(const typename Op::T (&v)[CHUNKS * EPC], uint32_t hb,
+                                                     uint32_t rrot, typename Op::S (&ca)[CHUNKS]) {
+    using S = typename Op::S;
+    uint32_t mask = 0;
+#pragma unroll
+    for (int c = 0; c < CHUNKS; ++c) {
+        const uint32_t bits = chunk_head_bits<Op, CHUNKS, EPC, SEG>(hb, c, rrot);
+        S x = Op::zero();
+#pragma unroll
+        for (int e = 0; e < EPC; ++e) x = ((bits >> e) & 1u) ? Op::lift(v[c * EPC + e]) : Op::acc(x, v[c * EPC + e]);
+        ca[c] = x;
+        mask |= (bits != 0u ? 1u : 0u) << c;
+    }
+    if (REORDER) {
+        rotate_chunks<S, CHUNKS, 1>(ca, rrot);
+        mask = ((mask << rrot) | (mask >> ((CHUNKS - rrot) & (CHUNKS - 1)))) & ((1u << CHUNKS) - 1u);
+    }
+    return mask;
+}
+
+// Outputs of a thread's items from the state before each chunk (cp, in
+// register order): CHUNKS independent chains of EPC items.
+template <class Op, int CHUNKS, int EPC, bool SEG, bool INCL>
+__device__ __forceinline__ void chunk_outputs(typename Op::T (&v)[CHUNKS * EPC], const typename Op::S (&cp)[CHUNKS],
+                                              uint32_t hb, uint32_t rrot) {
+    using S = typename Op::S;
+#pragma unroll
+    for (int c = 0; c < CHUNKS; ++c) {
+        const uint32_t bits = chunk_head_bits<Op, CHUNKS, EPC, SEG>(hb, c, rrot);
+        S st = cp[c];
+#pragma unroll
+        for (int e = 0; e < EPC; ++e) {
+            const S before = ((bits >> e) & 1u) ? Op::zero() : st;
+            st = Op::acc(before, v[c * EPC + e]);
+            v[c * EPC + e] = INCL ? Op::out(st) : Op::out(before);
+        }
+    }
 }
 
 // Lookback over 128-bit generic descriptors (see lookback() in
@@ -157,7 +212,7 @@ __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t e
     }
 }
 
-template <class Op, int RW, int RS, int SS, int Q, int G>
+template <class Op, int RW, int RS, int SS, int Q, int G, bool SEG>
 struct SegCtrl {
     using S = typename Op::S;
     using C = typename Op::C;
@@ -176,14 +231,15 @@ struct SegCtrl {
     uint32_t r_wflag[2][RW];
     S f_wtot[2][RW];
     uint32_t f_wflag[2][RW];
-    uint32_t heads[Q][G][kHeadWords];  // bit b of word w: element 32w+b is a segment head
-    uint32_t sample[1024];             // offsets[j * sample_stride], to start head searches
+    // Segmented scans only (one unused entry otherwise):
+    uint32_t heads[SEG ? Q : 1][G][kHeadWords];  // bit b of word w: element 32w+b is a segment head
+    uint32_t sample[SEG ? 1024 : 1];             // offsets[j * sample_stride], to start head searches
 };
 
-template <class Op, int RW, int RS, int SS, int Q, int G>
+template <class Op, int RW, int RS, int SS, int Q, int G, bool SEG>
 constexpr size_t seg_smem_bytes() {
     return static_cast<size_t>(RS + SS) * TileShape<typename Op::T, RW>::kTile * sizeof(typename Op::T) +
-           sizeof(SegCtrl<Op, RW, RS, SS, Q, G>);
+           sizeof(SegCtrl<Op, RW, RS, SS, Q, G, SEG>);
 }
 
 template <class Op, int RW>
@@ -208,7 +264,10 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     constexpr int kHeadWords = TILE / 32;
     static_assert(CHUNKS == 8, "128 bytes per thread");
     static_assert(Q > LW, "every lookback warp needs its own queue entry");
-    using Ctrl = SegCtrl<Op, RW, RS, SS, Q, G>;
+    using Ctrl = SegCtrl<Op, RW, RS, SS, Q, G, SEG>;
+    // Chunk aggregates go in logical order for segmented scans (heads) and
+    // for floating point (one summation order in both passes).
+    constexpr bool REORDER = SEG || !std::is_integral<T>::value;
 
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     T* rbuf = reinterpret_cast<T*>(smem_raw);
@@ -258,6 +317,8 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     auto wait1 = [&](uint64_t* bar, uint32_t ph, uint64_t b) -> bool {
         return ptx::mbar_try_wait(bar, ph) || ptx::mbar_wait_bounded(bar, ph, ptx::global_timer_ns() + b);
     };
+    // Head-bit words of tile k of queue entry q (segmented scans only).
+    auto heads_of = [&](int q, int k) -> uint32_t* { return ctrl->heads[SEG ? q : 0][k]; };
     // Head bits of a thread's ITEMS consecutive items (logical order).
     auto head_bits = [&](const uint32_t* hw, uint32_t thr) -> uint32_t {
         if (!SEG) return 0u;
@@ -420,6 +481,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     }
     // ======================================================== head warp
     else if (warp == 3) {
+        constexpr int kHeadBatch = 8;  // offset loads in flight per lane
         // Unsegmented scans read no head bits; the warp has nothing to do
         // (it must not fall behind the queue phases, so it leaves).
         if (!SEG) return;
@@ -441,7 +503,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
             const uint32_t u = ctrl->unit_of[q];
             if (u == kTileEnd) break;
             for (int k = 0; k < G; ++k)
-                for (int w = lane; w < kHeadWords; w += 32) ctrl->heads[q][k][w] = 0u;
+                for (int w = lane; w < kHeadWords; w += 32) heads_of(q, k)[w] = 0u;
             __syncwarp();
             if (SEG && nseg != 0) {
                 const uint64_t ustart = static_cast<uint64_t>(u) * G * TILE;
@@ -455,19 +517,39 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                     else
                         hi_s = mid;
                 }
-                // Segments [base, base + stride) hold the first offset >= ustart.
-                uint32_t cur = lo_s == 0 ? 0u : (lo_s - 1) * stride;
-                // Walk forward over offsets[cur..nseg-1], 32 at a time.
-                while (cur < nseg) {
-                    const uint32_t idx = cur + lane;
-                    const uint32_t o = idx < nseg ? sg.offsets[idx] : 0xFFFFFFFFu;
-                    if (o >= ustart && o < uend) {
-                        const uint32_t pos = static_cast<uint32_t>(o - ustart);
-                        atomicOr(&ctrl->heads[q][pos / TILE][(pos % TILE) >> 5], 1u << (pos & 31u));
+                // The first offset >= ustart has an index in [lo_i, hi_i].
+                uint32_t lo_i = lo_s == 0 ? 0u : (lo_s - 1) * stride;
+                uint32_t hi_i = lo_s < nsample ? min(lo_s * stride, nseg) : nseg;
+                // Narrow a wide interval (many short segments) 32-fold per
+                // round: one offset per lane, the last lane below ustart wins.
+                while (hi_i - lo_i > kHeadBatch * 32u) {
+                    const uint32_t step = (hi_i - lo_i + 31u) / 32u;
+                    const uint32_t idx = min(lo_i + lane * step, nseg - 1u);
+                    const uint32_t below = __ballot_sync(kFullMask, sg.offsets[idx] < ustart);
+                    if (below == 0u) break;  // offsets[lo_i] >= ustart already
+                    const uint32_t last = 31u - static_cast<uint32_t>(__clz(below));
+                    hi_i = min(lo_i + (last + 1u) * step, hi_i);
+                    lo_i = lo_i + last * step;
+                }
+                // Walk forward from lo_i, kHeadBatch loads of 32 offsets in
+                // flight per round, until an offset at or past uend.
+                for (uint32_t cur = lo_i; cur < nseg; cur += kHeadBatch * 32u) {
+                    uint32_t o[kHeadBatch];
+#pragma unroll
+                    for (int j = 0; j < kHeadBatch; ++j) {
+                        const uint32_t idx = cur + static_cast<uint32_t>(j) * 32u + lane;
+                        o[j] = idx < nseg ? sg.offsets[idx] : 0xFFFFFFFFu;
                     }
-                    const bool past = __ballot_sync(kFullMask, o >= uend) != 0;
-                    if (past) break;
-                    cur += 32;
+                    bool past = false;
+#pragma unroll
+                    for (int j = 0; j < kHeadBatch; ++j) {
+                        if (o[j] >= ustart && o[j] < uend) {
+                            const uint32_t pos = static_cast<uint32_t>(o[j] - ustart);
+                            atomicOr(&heads_of(q, static_cast<int>(pos / TILE))[(pos % TILE) >> 5], 1u << (pos & 31u));
+                        }
+                        past = past || o[j] >= uend;
+                    }
+                    if (__any_sync(kFullMask, past)) break;
                 }
             }
             __syncwarp();
@@ -557,9 +639,6 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
 #pragma unroll
                     for (int e = 0; e < EPC; ++e) v[c8 * EPC + e] = qv.v[e];
                 }
-                // Logical order: for the heads, and so that floating-point
-                // sums are formed exactly as the finalize warps form them.
-                if (SEG || !std::is_integral<T>::value) rotate_chunks<T, CHUNKS, EPC>(v, rot);
             } else {
                 const uint32_t bulk_elems = live ? bulk_bytes_of(t) / static_cast<uint32_t>(sizeof(T)) : 0u;
                 const uint64_t gbase = static_cast<uint64_t>(live ? t : 0u) * TILE;
@@ -574,16 +653,23 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                     v[e] = x;
                 }
             }
-            const uint32_t hb = live ? head_bits(ctrl->heads[q][k], r) : 0u;
-            // Thread aggregate (items beyond cnt are zero and carry no head).
+            const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), r) : 0u;
+            const uint32_t rrot = cnt == static_cast<uint32_t>(TILE) ? rot : 0u;
+            // Thread aggregate (items beyond cnt are zero and carry no head),
+            // formed exactly as the finalize warps form it: chunk aggregates
+            // combined in logical order (integer sums need no order).
+            // Warps whose items hold no segment head take the plain path.
+            S ca[CHUNKS];
+            const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
+            const uint32_t cmask = heads_here
+                                       ? chunk_aggregates<Op, CHUNKS, EPC, SEG, REORDER>(v, hb, rrot, ca)
+                                       : chunk_aggregates<Op, CHUNKS, EPC, false, !std::is_integral<T>::value>(
+                                             v, 0u, rrot, ca);
             S tv = Op::zero();
             bool tf = false;
 #pragma unroll
-            for (int e = 0; e < ITEMS; ++e) {
-                const bool h = (hb >> e) & 1u;
-                tv = h ? Op::lift(v[e]) : Op::add(tv, Op::lift(v[e]));
-                tf = tf || h;
-            }
+            for (int c = 0; c < CHUNKS; ++c) seg_combine<Op>(tv, tf, ca[c], (cmask >> c) & 1u);
+            tv = Op::norm(tv);
             // Warp aggregate: inclusive segmented scan, lane 31 holds it.
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
@@ -661,7 +747,6 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
 #pragma unroll
                     for (int e = 0; e < EPC; ++e) v[c8 * EPC + e] = qv.v[e];
                 }
-                rotate_chunks<T, CHUNKS, EPC>(v, rot);  // logical order
             } else {
 #pragma unroll
                 for (int e = 0; e < ITEMS; ++e) {
@@ -681,15 +766,17 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                 hok = ptx::mbar_try_wait(&ctrl->uheads[q], (i / Q) & 1u) ||
                       ptx::mbar_wait_bounded(&ctrl->uheads[q], (i / Q) & 1u, ptx::global_timer_ns() + long_budget);
             if (!hok) raise_error(a.hdr, kErrPipelineTimeout);
-            const uint32_t hb = live ? head_bits(ctrl->heads[q][k], f) : 0u;
+            const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), f) : 0u;
+            const uint32_t rrot = full_tile ? rot : 0u;
+            S ca[CHUNKS];
+            const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
+            const uint32_t cmask = heads_here ? chunk_aggregates<Op, CHUNKS, EPC, SEG, REORDER>(v, hb, rrot, ca)
+                                              : chunk_aggregates<Op, CHUNKS, EPC, false, REORDER>(v, 0u, rrot, ca);
             S tv = Op::zero();
             bool tf = false;
 #pragma unroll
-            for (int e = 0; e < ITEMS; ++e) {
-                const bool h = (hb >> e) & 1u;
-                tv = h ? Op::lift(v[e]) : Op::add(tv, Op::lift(v[e]));
-                tf = tf || h;
-            }
+            for (int c = 0; c < CHUNKS; ++c) seg_combine<Op>(tv, tf, ca[c], (cmask >> c) & 1u);
+            tv = Op::norm(tv);
             // Exclusive segmented scan of thread aggregates within the warp.
             S wv = tv;
             bool wf = tf;
@@ -745,16 +832,24 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                 bool rf = false;
                 seg_combine<Op>(run, rf, tile_agg, tile_f);
             }
-            S st = base;
+            // State before each chunk (logical order), then back to register
+            // order; then CHUNKS independent chains of EPC items.
+            {
+                S st = base;
+                bool sf = false;
 #pragma unroll
-            for (int e = 0; e < ITEMS; ++e) {
-                const bool h = (hb >> e) & 1u;
-                const S before = h ? Op::zero() : st;
-                st = Op::add(before, Op::lift(v[e]));
-                v[e] = INCL ? Op::out(st) : Op::out(before);
+                for (int c = 0; c < CHUNKS; ++c) {
+                    const S x = ca[c];
+                    ca[c] = st;
+                    seg_combine<Op>(st, sf, x, (cmask >> c) & 1u);
+                }
             }
+            if (REORDER) rotate_chunks<S, CHUNKS, 1>(ca, (CHUNKS - rrot) & (CHUNKS - 1));
+            if (heads_here)
+                chunk_outputs<Op, CHUNKS, EPC, SEG, INCL>(v, ca, hb, rrot);
+            else
+                chunk_outputs<Op, CHUNKS, EPC, false, INCL>(v, ca, 0u, rrot);
             if (full_tile) {
-                rotate_chunks<T, CHUNKS, EPC>(v, (CHUNKS - rot) & (CHUNKS - 1));  // back to stored order
 #pragma unroll
                 for (int c8 = 0; c8 < CHUNKS; ++c8) {
                     const uint32_t c = (c8 + rot) & (CHUNKS - 1);

@@ -7,11 +7,11 @@
 
 namespace gps {
 
-// 4 reduce + 4 finalize warps over 16 KB tiles, 4 reduce-pass and 8
+// 4 reduce + 4 finalize warps over 16 KB tiles, 5 reduce-pass and 8
 // scan-pass stages, units of 4 tiles, 6 units in flight per CTA (the
 // measured optimum of the u32 L2-buffered kernel, scan_l2.cuh).
 constexpr int kSegWarps = 4;
-constexpr int kSegRStages = 4;
+constexpr int kSegRStages = 5;
 constexpr int kSegSStages = 8;
 constexpr int kSegQueue = 6;
 constexpr int kSegUnit = 4;
@@ -19,7 +19,8 @@ constexpr int kSegUnit = 4;
 template <class Op, bool INCL, bool SEG>
 cudaError_t launch_seg_t(const ScanArgs& a, const SegArgs& sg, int num_sms, cudaStream_t stream, LaunchInfo* info) {
     auto kern = scan_seg_kernel<Op, kSegWarps, kSegRStages, kSegSStages, kSegQueue, kSegUnit, INCL, SEG>;
-    constexpr size_t smem = seg_smem_bytes<Op, kSegWarps, kSegRStages, kSegSStages, kSegQueue, kSegUnit>();
+    constexpr size_t smem = seg_smem_bytes<Op, kSegWarps, kSegRStages, kSegSStages, kSegQueue, kSegUnit, SEG>();
+    static_assert(smem <= 232448, "227 KB of shared memory per CTA");
     constexpr int threads = SegShape<Op, kSegWarps>::kThreads;
     int occ = 0;
     cudaError_t err = resident_ctas_per_sm(kern, threads, smem, &occ);

@@ -41,9 +41,10 @@ class Plan:
 
     # -- lifetime
     def close(self) -> None:
-        if getattr(self, "_h", None) is not None and self._h.value:
-            check(lib.gps_plan_destroy(self._h), "gps_plan_destroy")
-            self._h = None
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._h = None  # never destroyed twice, even if destroy reports an error
+            check(lib.gps_plan_destroy(h), "gps_plan_destroy")
 
     def __del__(self):
         try:

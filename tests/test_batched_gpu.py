@@ -56,6 +56,23 @@ def test_segmented_random_lengths_bit_exact(cuda, dtype, inclusive):
     assert np.array_equal(got.cpu().numpy().view(NP[dtype]), want)
 
 
+@pytest.mark.parametrize("dtype", ["u32", "u64"])
+def test_segmented_many_short_segments(cuda, dtype):
+    # Hundreds of thousands of segments of 0..3 elements: every tile holds
+    # hundreds of heads, and the offsets between two samples are searched.
+    rng = np.random.default_rng(23)
+    lengths = rng.integers(0, 4, size=600_000)
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    x = rng.integers(0, np.iinfo(NP[dtype]).max, size=n, dtype=NP[dtype], endpoint=True)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    with Plan("csdl", dtype, max_n=n) as plan:
+        for inclusive in (False, True):
+            got = plan.scan_segmented(dev(x), d_off, inclusive=inclusive)
+            plan.check()
+            assert np.array_equal(got.cpu().numpy().view(NP[dtype]), oracle.segscan(x, offs, inclusive))
+
+
 def test_segmented_config3_4096_segments_in_place(cuda):
     lengths = config3_lengths()
     offs = offsets_of(lengths)
@@ -100,6 +117,29 @@ def test_segmented_equals_looped_plain_scans_and_replays_from_a_graph(cuda):
             torch.cuda.synchronize()
             assert torch.equal(out, looped)
         plan.check()
+
+
+@pytest.mark.parametrize("max_n", [3 * 4096, 5 * 4096 + 1, 1 << 20])
+def test_segmented_and_plain_scans_share_a_u32_plan(cuda, max_n):
+    # Plans whose tile count is odd or even; plain scans (8-byte descriptors)
+    # and batched scans (16-byte descriptors) alternate on the same plan.
+    rng = np.random.default_rng(max_n)
+    lengths = rng.integers(0, 3000, size=max_n // 1500)
+    lengths[-1] += max_n - lengths.sum() if lengths.sum() < max_n else 0
+    lengths = lengths[np.cumsum(lengths) <= max_n]
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    x = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    want_seg = oracle.segscan(x, offs, False)
+    want = oracle.scan(x, inclusive=True)
+    with Plan("csdl", "u32", max_n=max_n) as plan:
+        for _ in range(3):
+            seg = plan.scan_segmented(dev(x), d_off)
+            full = plan.scan(dev(x), inclusive=True)
+            plan.check()
+            assert np.array_equal(seg.cpu().numpy().view(np.uint32), want_seg)
+            assert np.array_equal(full.cpu().numpy().view(np.uint32), want)
 
 
 # ------------------------------------------------------------ floating point
