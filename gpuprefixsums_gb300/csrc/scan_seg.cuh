@@ -105,6 +105,63 @@ __device__ __forceinline__ uint32_t chunk_aggregates(const typename Op::T (&v)[C
     return mask;
 }
 
+// Inclusive warp scan of (state, head flag) in lane order. Without FLAGS the
+// flags are known to be false and only the states move.
+template <class Op, bool FLAGS>
+__device__ __forceinline__ void warp_scan_incl(typename Op::S& s, bool& f, uint32_t lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const typename Op::S ov = Op::shfl_up(s, d);
+        const bool of = FLAGS ? __shfl_up_sync(kFullMask, f, d) : false;
+        if (lane >= static_cast<uint32_t>(d)) {
+            if (FLAGS) {
+                s = f ? s : Op::combine(ov, s);
+                f = f || of;
+            } else {
+                s = Op::combine(ov, s);
+            }
+        }
+    }
+}
+
+// Sum of a warp's states in every lane, in no particular order (wrapping
+// integer sums only).
+template <class Op>
+__device__ __forceinline__ typename Op::S warp_sum_unordered(typename Op::S s) {
+#pragma unroll
+    for (int m = 16; m; m >>= 1) s = Op::combine(s, Op::shfl(s, (threadIdx.x & 31u) ^ static_cast<uint32_t>(m)));
+    return s;
+}
+
+// Thread aggregate of a thread's items and the warp's inclusive scan of it;
+// HEADS = false when no item of the warp is a segment head. UNORDERED: only
+// the warp total is wanted and the type's sums need no order.
+template <class Op, int CHUNKS, int EPC, bool HEADS, bool REORDER, bool UNORDERED>
+__device__ __forceinline__ uint32_t thread_and_warp_scan(const typename Op::T (&v)[CHUNKS * EPC], uint32_t hb,
+                                                         uint32_t rrot, uint32_t lane, typename Op::S (&ca)[CHUNKS],
+                                                         typename Op::S& ws, bool& wf) {
+    using S = typename Op::S;
+    const uint32_t cmask = chunk_aggregates<Op, CHUNKS, EPC, HEADS, REORDER>(v, hb, rrot, ca);
+    S tv = Op::zero();
+    bool tf = false;
+#pragma unroll
+    for (int c = 0; c < CHUNKS; ++c) {
+        if (HEADS)
+            seg_combine<Op>(tv, tf, ca[c], (cmask >> c) & 1u);
+        else
+            tv = Op::combine(tv, ca[c]);
+    }
+    tv = Op::norm(tv);
+    if (UNORDERED && !HEADS) {
+        tv = warp_sum_unordered<Op>(tv);
+    } else {
+        warp_scan_incl<Op, HEADS>(tv, tf, lane);
+    }
+    ws = tv;
+    wf = tf;
+    return cmask;
+}
+
 // Outputs of a thread's items from the state before each chunk (cp, in
 // register order): CHUNKS independent chains of EPC items.
 template <class Op, int CHUNKS, int EPC, bool SEG, bool INCL>
@@ -265,8 +322,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     static_assert(CHUNKS == 8, "128 bytes per thread");
     static_assert(Q > LW, "every lookback warp needs its own queue entry");
     using Ctrl = SegCtrl<Op, RW, RS, SS, Q, G, SEG>;
-    // Chunk aggregates go in logical order for segmented scans (heads) and
-    // for floating point (one summation order in both passes).
+    // The reduce pass sums the chunk aggregates in logical order for
+    // segmented scans (heads) and for floating point (the summation order of
+    // the scan pass); wrapping integer sums need no order.
     constexpr bool REORDER = SEG || !std::is_integral<T>::value;
 
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -655,34 +713,18 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
             }
             const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), r) : 0u;
             const uint32_t rrot = cnt == static_cast<uint32_t>(TILE) ? rot : 0u;
-            // Thread aggregate (items beyond cnt are zero and carry no head),
-            // formed exactly as the finalize warps form it: chunk aggregates
-            // combined in logical order (integer sums need no order).
-            // Warps whose items hold no segment head take the plain path.
+            // Warp aggregate (items beyond cnt are zero and carry no head),
+            // formed exactly as the finalize warps form it for floating point:
+            // chunk aggregates in logical order, then a lane-order scan. Warps
+            // whose items hold no segment head take the plain path.
             S ca[CHUNKS];
-            const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
-            const uint32_t cmask = heads_here
-                                       ? chunk_aggregates<Op, CHUNKS, EPC, SEG, REORDER>(v, hb, rrot, ca)
-                                       : chunk_aggregates<Op, CHUNKS, EPC, false, !std::is_integral<T>::value>(
-                                             v, 0u, rrot, ca);
-            S tv = Op::zero();
-            bool tf = false;
-#pragma unroll
-            for (int c = 0; c < CHUNKS; ++c) seg_combine<Op>(tv, tf, ca[c], (cmask >> c) & 1u);
-            tv = Op::norm(tv);
-            // Warp aggregate: inclusive segmented scan, lane 31 holds it.
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const S ov = Op::shfl_up(tv, d);
-                const bool of = __shfl_up_sync(kFullMask, tf, d);
-                if (lane >= static_cast<uint32_t>(d)) {
-                    S x = ov;
-                    bool fx = of;
-                    seg_combine<Op>(x, fx, tv, tf);
-                    tv = x;
-                    tf = fx;
-                }
-            }
+            S tv;
+            bool tf;
+            if (SEG && __any_sync(kFullMask, hb != 0u))
+                thread_and_warp_scan<Op, CHUNKS, EPC, SEG, REORDER, false>(v, hb, rrot, lane, ca, tv, tf);
+            else
+                thread_and_warp_scan<Op, CHUNKS, EPC, false, !std::is_integral<T>::value,
+                                     std::is_integral<T>::value>(v, 0u, rrot, lane, ca, tv, tf);
             if (lane == 31) {
                 ctrl->r_wtot[rn & 1u][rw] = tv;
                 ctrl->r_wflag[rn & 1u][rw] = tf;
@@ -768,32 +810,17 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
             if (!hok) raise_error(a.hdr, kErrPipelineTimeout);
             const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), f) : 0u;
             const uint32_t rrot = full_tile ? rot : 0u;
+            // Chunk aggregates (logical order) and the warp's inclusive scan
+            // of the thread aggregates; then exclusive by one lane.
             S ca[CHUNKS];
+            S wv;
+            bool wf;
             const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
-            const uint32_t cmask = heads_here ? chunk_aggregates<Op, CHUNKS, EPC, SEG, REORDER>(v, hb, rrot, ca)
-                                              : chunk_aggregates<Op, CHUNKS, EPC, false, REORDER>(v, 0u, rrot, ca);
-            S tv = Op::zero();
-            bool tf = false;
-#pragma unroll
-            for (int c = 0; c < CHUNKS; ++c) seg_combine<Op>(tv, tf, ca[c], (cmask >> c) & 1u);
-            tv = Op::norm(tv);
-            // Exclusive segmented scan of thread aggregates within the warp.
-            S wv = tv;
-            bool wf = tf;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const S ov = Op::shfl_up(wv, d);
-                const bool of = __shfl_up_sync(kFullMask, wf, d);
-                if (lane >= static_cast<uint32_t>(d)) {
-                    S x = ov;
-                    bool fx = of;
-                    seg_combine<Op>(x, fx, wv, wf);
-                    wv = x;
-                    wf = fx;
-                }
-            }
+            const uint32_t cmask =
+                heads_here ? thread_and_warp_scan<Op, CHUNKS, EPC, SEG, true, false>(v, hb, rrot, lane, ca, wv, wf)
+                           : thread_and_warp_scan<Op, CHUNKS, EPC, false, true, false>(v, 0u, rrot, lane, ca, wv, wf);
             S xv = Op::shfl_up(wv, 1);
-            bool xf = __shfl_up_sync(kFullMask, wf, 1);
+            bool xf = SEG ? __shfl_up_sync(kFullMask, wf, 1) : false;
             if (lane == 0) {
                 xv = Op::zero();
                 xf = false;
@@ -844,7 +871,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                     seg_combine<Op>(st, sf, x, (cmask >> c) & 1u);
                 }
             }
-            if (REORDER) rotate_chunks<S, CHUNKS, 1>(ca, (CHUNKS - rrot) & (CHUNKS - 1));
+            rotate_chunks<S, CHUNKS, 1>(ca, (CHUNKS - rrot) & (CHUNKS - 1));
             if (heads_here)
                 chunk_outputs<Op, CHUNKS, EPC, SEG, INCL>(v, ca, hb, rrot);
             else
