@@ -17,7 +17,17 @@ Reported (one JSON line on rank 0):
                buffers (host->device and device->host copies timed);
   compare      D2D copy of the same bytes (the 100% line), CUB DeviceScan and
                the reduce-then-scan path on the same buffers;
-  cpu_baseline the oracle's serial scan on one host core.
+  cpu_baseline the oracle's serial scan on one host core;
+  batched      4096 independent u32 exclusive scans, lengths log-uniform in
+               [1, 2^20] (seeded), CSR offsets: one autotuned launch replayed
+               from a CUDA graph against a graph of one plain scan per segment
+               (identical output checked), speed-up and GB/s;
+  fp32         inclusive scans of 2^26 floats, N(0,1) and mixed magnitude
+               (|x| log-uniform in [1e-8, 1e8], random sign): plain and
+               compensated FP32 throughput and errors against a float64 scan;
+  mixed        10,000 scans, lengths Zipf(1.2) in [32, 2^22], dtype per scan
+               from {u32, u64, compensated f32}, plus a 2^28-element u32
+               Bernoulli(0.3) flag scan, all in one CUDA graph.
 With --impl reference the line times the reference's own algorithm on the
 host instead (the oracle's multi-threaded restatement, all host threads): the
 reference ships no CPU scan of its own.
@@ -53,6 +63,10 @@ def parse_args():
     p.add_argument("--algo", choices=["csdl", "rts"], default="csdl")
     p.add_argument("--no-compare", action="store_true",
                    help="only the timed scans (for profiling): no copy/CUB/RTS/e2e/CPU legs")
+    p.add_argument("--no-extras", action="store_true", help="skip the batched, fp32 and mixed workloads")
+    p.add_argument("--profile-case", choices=["batched", "f32c"], default=None,
+                   help="launch one small case of a generic-kernel workload three times and exit (ncu captures): "
+                        "1024 of the batched workload's segments, or 2^26 compensated-f32 elements")
     p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
@@ -191,6 +205,222 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- workload extras
+def graph_of(fn, stream):
+    """Captures fn (which launches on `stream`) in a CUDA graph; returns a
+    callable that replays it on `stream`."""
+    import torch
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        fn()  # warm-up outside the capture (first-use setup)
+        stream.synchronize()
+        with torch.cuda.graph(g, stream=stream):
+            fn()
+    stream.synchronize()
+
+    def replay():
+        with torch.cuda.stream(stream):  # replay() launches on the current stream
+            g.replay()
+    replay.graph = g
+    return replay
+
+
+def log_uniform_lengths(count, hi, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(0.0, np.log(float(hi)), size=count))).astype(np.int64)
+
+
+def zipf_lengths(count, s, lo, hi, seed):
+    """Continuous Zipf(s) (density ~ x^-s) truncated to [lo, hi], floored:
+    inverse CDF of a seeded uniform."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(0.0, 1.0, size=count)
+    a, b = lo ** (1.0 - s), hi ** (1.0 - s)
+    x = (a - u * (a - b)) ** (1.0 / (1.0 - s))
+    return np.clip(np.floor(x), lo, hi).astype(np.int64)
+
+
+def run_batched(stream, copy_gbs, reps=20):
+    """4096 u32 exclusive scans in one launch vs one plain launch per scan."""
+    import numpy as np
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    lengths = log_uniform_lengths(4096, 2 ** 20, seed=3)
+    offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint32)
+    n = int(offs[-1])
+    gen = torch.Generator(device="cuda").manual_seed(4096)
+    x = torch.randint(0, 256, (n,), dtype=torch.int32, device="cuda", generator=gen)
+    d_off = torch.from_numpy(offs.view(np.int32)).cuda()
+    out_b, out_l = torch.empty_like(x), torch.empty_like(x)
+    segs = [(int(offs[i]), int(offs[i + 1])) for i in range(len(lengths)) if offs[i + 1] > offs[i]]
+    with Plan("csdl", "u32", max_n=n) as plan:
+        tuned = plan.autotune(x, d_off, out=out_b, stream=stream)
+        gb = graph_of(lambda: plan.scan_segmented(x, d_off, out=out_b, stream=stream), stream)
+        xp, op = x.data_ptr(), out_l.data_ptr()
+
+        def looped():
+            for b, e in segs:
+                plan.scan_ptr(xp + 4 * b, op + 4 * b, e - b, stream=stream)
+        gl = graph_of(looped, stream)
+        for _ in range(3):
+            gb()
+        ms_b = time_loop(gb, reps, stream)
+        gl()
+        ms_l = time_loop(gl, 3, stream)
+        looped()
+        ms_e = time_loop(looped, 2, stream)
+        plan.check(stream)
+        same = bool(torch.equal(out_b, out_l))
+    if not same:
+        raise SystemExit("bench: batched and looped scans differ; refusing to report a number")
+    alg = n * 8 + 4 * len(offs)
+    gbs = alg / (ms_b * 1e-3) / 1e9
+    return {"workload": "4096 u32 exclusive scans, lengths floor(log-uniform[1, 2^20]) seed 3, values uniform "
+                        "[0,255], CSR uint32 offsets; batched = 1 launch replayed from a CUDA graph",
+            "elements": n, "segments": len(lengths), "ms_batched": round(ms_b, 4),
+            "ms_looped_graph": round(ms_l, 3), "ms_looped_eager": round(ms_e, 3),
+            "speedup_vs_looped_graph": round(ms_l / ms_b, 2), "speedup_vs_looped_eager": round(ms_e / ms_b, 2),
+            "gbs": round(gbs, 2), "pct_of_copy": round(100.0 * gbs / copy_gbs, 2) if copy_gbs else None,
+            "identical_to_looped": same, "autotuned": tuned, "launches_per_step": 1}
+
+
+def fp_errors_vs_f64(got, ref):
+    """max / median relative prefix error (nonzero reference prefixes) and
+    relative error of the final sum, against a float64 scan."""
+    import torch
+    g = got.double()
+    nz = ref != 0
+    rel = (g[nz] - ref[nz]).abs() / ref[nz].abs()
+    fin = float(((g[-1] - ref[-1]).abs() / ref[-1].abs()).item()) if float(ref[-1]) != 0 else None
+    return {"max_rel": float(rel.max().item()), "median_rel": float(torch.median(rel).item()),
+            "final_sum_rel": fin}
+
+
+def run_fp32(stream, reps=20):
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    n = 1 << 26
+    gen = torch.Generator(device="cuda").manual_seed(26)
+    sets = {"normal": torch.randn(n, device="cuda", generator=gen)}
+    mag = torch.exp(torch.empty(n, device="cuda", dtype=torch.float64).uniform_(
+        float(torch.log(torch.tensor(1e-8, dtype=torch.float64))),
+        float(torch.log(torch.tensor(1e8, dtype=torch.float64))), generator=gen))
+    sign = torch.where(torch.rand(n, device="cuda", generator=gen) < 0.5, -1.0, 1.0).double()
+    sets["mixed"] = (mag * sign).float()
+    del mag, sign
+    res = {"workload": "inclusive scans of 2^26 float32, N(0,1) and |x| log-uniform [1e-8,1e8] with random sign; "
+                       "errors against torch.cumsum in float64 on the same inputs",
+           "n": n}
+    out = torch.empty(n, device="cuda")
+    for name, x in sets.items():
+        ref = torch.cumsum(x.double(), 0)
+        row = {}
+        for dt in ("f32", "f32c"):
+            with Plan("csdl", dt, max_n=n) as plan:
+                step = lambda: plan.scan(x, out, inclusive=True, stream=stream)  # noqa: E731
+                for _ in range(3):
+                    step()
+                ms = time_loop(step, reps, stream)
+                plan.check(stream)
+                row[dt] = {"gbs": round(n * 8 / (ms * 1e-3) / 1e9, 2), "ms": round(ms, 4),
+                           **fp_errors_vs_f64(out, ref)}
+        row["compensated_cost_pct"] = round(100.0 * (row["f32"]["gbs"] / row["f32c"]["gbs"] - 1.0), 1)
+        res[name] = row
+    return res
+
+
+def run_mixed(stream, copy_gbs, reps=5):
+    """Config of 10,000 mixed-dtype scans plus a 2^28 flag scan, one graph."""
+    import numpy as np
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    count = 10_000
+    lengths = zipf_lengths(count, 1.2, 32, 2 ** 22, seed=5)
+    kinds = np.random.default_rng(55).integers(0, 3, size=count)  # 0 u32, 1 u64, 2 f32c
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    groups = {}
+    for k, (name, tdt) in enumerate((("u32", torch.int32), ("u64", torch.int64), ("f32c", torch.float32))):
+        ls = lengths[kinds == k]
+        offs = np.concatenate([[0], np.cumsum(ls)]).astype(np.uint32)
+        m = int(offs[-1])
+        if name == "u32":
+            x = torch.randint(0, 256, (m,), dtype=tdt, device="cuda", generator=gen)
+        elif name == "u64":
+            x = torch.randint(-2 ** 63, 2 ** 63 - 1, (m,), dtype=tdt, device="cuda", generator=gen)
+        else:
+            x = torch.randn(m, device="cuda", generator=gen)
+        groups[name] = {"x": x, "out": torch.empty_like(x), "offs": torch.from_numpy(offs.view(np.int32)).cuda(),
+                        "offs_host": offs, "plan": Plan("csdl", name, max_n=m), "m": m, "scans": len(ls)}
+    nf = 1 << 28
+    flags = (torch.rand(nf, device="cuda", generator=gen) < 0.3).to(torch.int32)
+    fout = torch.empty_like(flags)
+    fplan = Plan("csdl", "u32", max_n=nf)
+    for g in groups.values():
+        g["plan"].autotune(g["x"], g["offs"], out=g["out"], stream=stream)
+
+    def batch():
+        for g in groups.values():
+            g["plan"].scan_segmented(g["x"], g["offs"], out=g["out"], stream=stream)
+        fplan.scan(flags, fout, inclusive=False, stream=stream)
+    graph = graph_of(batch, stream)
+    graph()
+    ms = time_loop(graph, reps, stream)
+    for g in groups.values():
+        g["plan"].check(stream)
+    fplan.check(stream)
+    # Exactness of the integer groups and the flag scan (difference property),
+    # error of the float group against per-segment float64 scans.
+    ok = True
+    ok &= bool((groups["f32c"]["out"][torch.from_numpy(groups["f32c"]["offs_host"][:-1].astype(np.int64)).cuda()]
+                == 0).all())
+    for name in ("u32", "u64"):
+        g = groups[name]
+        o, x, offs = g["out"], g["x"], g["offs_host"]
+        if name == "u32":
+            d = (o[1:].to(torch.int64) - o[:-1].to(torch.int64)) & 0xFFFFFFFF
+            want = x[:-1].to(torch.int64)
+        else:
+            d, want = o[1:] - o[:-1], x[:-1]
+        starts = torch.from_numpy(offs[1:-1].astype(np.int64)).cuda()
+        inner = torch.ones(g["m"] - 1, dtype=torch.bool, device="cuda")
+        inner[starts[starts > 0] - 1] = False
+        ok &= bool(torch.equal(d[inner], want[inner])) and bool((o[starts.clamp(max=g["m"] - 1)] == 0).all())
+    d = fout[1:] - fout[:-1]
+    ok &= int(fout[0]) == 0 and bool(torch.equal(d, flags[:-1]))
+    if not ok:
+        raise SystemExit("bench: mixed batch result is wrong; refusing to report a number")
+    g = groups["f32c"]
+    worst, med = 0.0, []
+    offs = g["offs_host"]
+    for i in range(len(offs) - 1):
+        b, e = int(offs[i]), int(offs[i + 1])
+        if e > b:
+            incl = torch.cumsum(g["x"][b:e].double(), 0)
+            err = fp_errors_vs_f64(g["out"][b + 1:e], incl[:-1])  # exclusive: out[b] == 0 is checked above
+            worst = max(worst, err["max_rel"])
+            med.append(err["median_rel"])
+    elems = sum(g["m"] for g in groups.values()) + nf
+    alg = sum(g["m"] * g["x"].element_size() * 2 + 4 * len(g["offs_host"]) for g in groups.values()) + nf * 8
+    gbs = alg / (ms * 1e-3) / 1e9
+    res = {"workload": "10,000 scans, lengths Zipf(1.2) floored in [32, 2^22] seed 5, dtype per scan uniform over "
+                       "{u32 [0,255], u64 full range, compensated f32 N(0,1)}, batched per dtype; plus an exclusive "
+                       "scan of 2^28 u32 Bernoulli(0.3) flags; 4 launches in one CUDA graph",
+           "scans": {k: g["scans"] for k, g in groups.items()}, "elements": elems, "ms": round(ms, 3),
+           "elements_per_s": round(elems / (ms * 1e-3), 1), "gbs": round(gbs, 2),
+           "pct_of_copy": round(100.0 * gbs / copy_gbs, 2) if copy_gbs else None,
+           "f32c_max_rel_err": worst, "f32c_median_rel_err": float(np.median(med)), "exact_integer_groups": ok,
+           "launches_per_step": 4}
+    for g in groups.values():
+        g["plan"].close()
+    fplan.close()
+    return res
+
+
 # ------------------------------------------------------------------ ours
 def run_ours(args, world, rank, local):
     import numpy as np
@@ -251,7 +481,7 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = measured_peak()
     kernel_gbs = alg_bytes / (ms / launches * 1e-3) / 1e9 if launches == 1 else None
 
-    compare, e2e, cpu = {}, None, None
+    compare, e2e, cpu, extras = {}, None, None, {}
     if not args.no_compare:
         reps = 30
 
@@ -308,6 +538,11 @@ def run_ours(args, world, rank, local):
                "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_s * 1e3, 3),
                "path": "gps_scan_host: pinned host -> device -> host, chunked and overlapped"}
 
+        if not args.no_extras:
+            extras["batched"] = run_batched(stream, compare.get("d2d_copy_gbs"))
+            extras["fp32"] = run_fp32(stream)
+            extras["mixed"] = run_mixed(stream, compare.get("d2d_copy_gbs"))
+
         if rank == 0 and world == 1:
             import oracle
             x = h_in.numpy().view(np.uint32)
@@ -348,13 +583,46 @@ def run_ours(args, world, rank, local):
         line["e2e"] = e2e
     if cpu:
         line["cpu_baseline"] = cpu
+    line.update(extras)
+    if "batched" in extras:
+        line["batched_vs_looped_speedup"] = extras["batched"]["speedup_vs_looped_graph"]
     print(json.dumps(line), flush=True)
     plan.close()
+
+
+def run_profile_case(args):
+    import numpy as np
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    if args.profile_case == "batched":
+        lengths = log_uniform_lengths(4096, 2 ** 20, seed=3)[:1024]
+        offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint32)
+        n = int(offs[-1])
+        x = torch.randint(0, 256, (n,), dtype=torch.int32, device="cuda")
+        d_off = torch.from_numpy(offs.view(np.int32)).cuda()
+        with Plan("csdl", "u32", max_n=n) as plan:
+            for _ in range(3):
+                out = plan.scan_segmented(x, d_off)
+            plan.check()
+    else:
+        n = 1 << 26
+        x = torch.randn(n, device="cuda")
+        with Plan("csdl", "f32c", max_n=n) as plan:
+            for _ in range(3):
+                out = plan.scan(x, inclusive=True)
+            plan.check()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": args.profile_case, "n": n, "launches": 3, "checksum": float(out[-1].item())}))
 
 
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
+    if args.profile_case:
+        sys.path.insert(0, ROOT)
+        run_profile_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
         return

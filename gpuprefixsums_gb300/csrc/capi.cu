@@ -18,6 +18,17 @@
 
 #include "gps_internal.h"
 
+// Size classes of the autotuner: n within a factor of four share a class.
+constexpr int kSizeClasses = 17;
+inline int size_class(uint64_t n) {
+    int bits = 0;
+    while (n > 1 && bits < 64) {
+        n >>= 1;
+        ++bits;
+    }
+    return std::min(kSizeClasses - 1, bits / 2);
+}
+
 struct gps_plan_s {
     gps_algo algo;
     gps_dtype dtype;
@@ -37,6 +48,9 @@ struct gps_plan_s {
     // u32 kernel; on other plans they are hdr and area.
     gps::WsHeader* hdr16;
     void* desc16;
+    // Autotuned launch configuration of the generic kernel per [segmented?]
+    // [size class] (index into gps::kGenericCandidates; -1: not tuned).
+    int8_t tuned[2][kSizeClasses];
     uint64_t wait_budget_ns;
     gps::StallConfig stall;
     gps::LaunchInfo last_launch;
@@ -76,14 +90,22 @@ bool valid_dtype(int d) {
 }
 bool is_float(gps_dtype d) { return d == GPS_DTYPE_F32 || d == GPS_DTYPE_F32_COMPENSATED; }
 
+// Launch configuration of the generic kernel for a scan of n elements: the
+// autotuned one of the size class if there is one, else the default rule.
+gps::GenericConfig generic_config(const gps_plan_s* p, bool segmented, uint64_t n) {
+    const int c = p->tuned[segmented ? 1 : 0][size_class(n)];
+    if (c >= 0 && c < gps::kNumGenericCandidates) return gps::kGenericCandidates[c];
+    return gps::default_generic_config(n, p->tile_elems, p->num_sms);
+}
+
 // Generic kernel (scan_seg.cuh): floating-point scans and batched scans.
 cudaError_t launch_generic(gps_dtype dtype, bool inclusive, const gps::ScanArgs& a, const gps::SegArgs* sg,
-                           int num_sms, cudaStream_t stream, gps::LaunchInfo* info) {
+                           const gps::GenericConfig& cfg, int num_sms, cudaStream_t stream, gps::LaunchInfo* info) {
     switch (dtype) {
-        case GPS_DTYPE_U32: return gps::launch_seg_u32(inclusive, a, sg, num_sms, stream, info);
-        case GPS_DTYPE_U64: return gps::launch_seg_u64(inclusive, a, sg, num_sms, stream, info);
-        case GPS_DTYPE_F32: return gps::launch_seg_f32(inclusive, a, sg, num_sms, stream, info);
-        case GPS_DTYPE_F32_COMPENSATED: return gps::launch_seg_f32c(inclusive, a, sg, num_sms, stream, info);
+        case GPS_DTYPE_U32: return gps::launch_seg_u32(inclusive, a, sg, cfg, num_sms, stream, info);
+        case GPS_DTYPE_U64: return gps::launch_seg_u64(inclusive, a, sg, cfg, num_sms, stream, info);
+        case GPS_DTYPE_F32: return gps::launch_seg_f32(inclusive, a, sg, cfg, num_sms, stream, info);
+        case GPS_DTYPE_F32_COMPENSATED: return gps::launch_seg_f32c(inclusive, a, sg, cfg, num_sms, stream, info);
     }
     return cudaErrorInvalidValue;
 }
@@ -118,7 +140,8 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     if (is_float(p->dtype)) {
         a.hdr = p->hdr16;
         a.desc = p->desc16;
-        err = launch_generic(p->dtype, inclusive, a, nullptr, p->num_sms, stream, &p->last_launch);
+        err = launch_generic(p->dtype, inclusive, a, nullptr, generic_config(p, false, n), p->num_sms, stream,
+                             &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
         err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0, a, p->num_sms, stream, &p->last_launch);
     } else {
@@ -132,6 +155,10 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
 
 namespace gps {
 size_t dtype_size(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 8 : 4; }
+GenericConfig default_generic_config(uint64_t n, uint32_t tile_elems, int num_sms) {
+    const uint64_t units4 = (n + 4ull * tile_elems - 1) / (4ull * tile_elems);
+    return units4 >= 2ull * static_cast<uint64_t>(num_sms) ? GenericConfig{4, 1} : GenericConfig{1, 1};
+}
 void record_error(const char* msg) { g_last_error = msg; }
 }  // namespace gps
 
@@ -177,6 +204,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->tile_elems = tile;
     p->capacity_tiles = tiles;
     p->wait_budget_ns = kDefaultBudgetNs;
+    std::memset(p->tuned, -1, sizeof(p->tuned));
     cudaError_t err = cudaGetDevice(&p->device);
     if (err == cudaSuccess) err = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (err != cudaSuccess) {
@@ -278,25 +306,30 @@ gps_status gps_scan(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_ou
                        reinterpret_cast<cudaStream_t>(stream));
 }
 
-gps_status gps_scan_segmented(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
-                              const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream) {
+namespace {
+
+// Validates a batched (d_offsets != NULL) or generic-kernel plain scan and
+// fills its kernel arguments. Returns GPS_OK with n == 0 meaning "nothing to do".
+gps_status prepare_generic(gps_plan_s* p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                           const uint32_t* d_offsets, uint64_t num_segments, gps::ScanArgs* a, gps::SegArgs* sg) {
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
     if (p->algo != GPS_ALGO_CSDL)
         return fail(GPS_ERR_UNSUPPORTED, "batched scans run on chained-scan plans (GPS_ALGO_CSDL)");
+    if (d_offsets == nullptr && !is_float(p->dtype))
+        return fail(GPS_ERR_UNSUPPORTED, "integer plans use the generic kernel for batched scans only");
     if (n == 0) return GPS_OK;
-    if (num_segments == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "%llu elements but no segments",
-                                       static_cast<unsigned long long>(n));
+    if (d_offsets != nullptr && num_segments == 0)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "%llu elements but no segments", static_cast<unsigned long long>(n));
     if (n > p->max_n)
         return fail(GPS_ERR_SIZE_EXCEEDS_PLAN, "requested size %llu exceeds the plan's maximum %llu",
                     static_cast<unsigned long long>(n), static_cast<unsigned long long>(p->max_n));
-    if (n > 0xFFFFFFFFull || num_segments > 0xFFFFFFFEull)
+    if (d_offsets != nullptr && (n > 0xFFFFFFFFull || num_segments > 0xFFFFFFFEull))
         return fail(GPS_ERR_INVALID_ARGUMENT, "uint32 offsets limit a batch to 2^32 - 1 elements");
-    if (d_in == nullptr || d_out == nullptr || d_offsets == nullptr)
-        return fail(GPS_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (d_in == nullptr || d_out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL pointer");
     const size_t es = gps::dtype_size(p->dtype);
     const uintptr_t i = reinterpret_cast<uintptr_t>(d_in), o = reinterpret_cast<uintptr_t>(d_out);
-    if (((i | o) & 15u) != 0) return fail(GPS_ERR_INVALID_ARGUMENT, "batched scans need 16-byte aligned buffers");
+    if (((i | o) & 15u) != 0) return fail(GPS_ERR_INVALID_ARGUMENT, "this scan needs 16-byte aligned buffers");
     if ((reinterpret_cast<uintptr_t>(d_offsets) & 3u) != 0)
         return fail(GPS_ERR_INVALID_ARGUMENT, "offsets must be 4-byte aligned");
     const uint64_t bytes = n * es;
@@ -304,20 +337,100 @@ gps_status gps_scan_segmented(gps_plan p, gps_scan_kind kind, const void* d_in, 
         return fail(GPS_ERR_INVALID_ARGUMENT, "input and output overlap without being identical");
     gps_status st = check_device(p);
     if (st != GPS_OK) return st;
-    gps::ScanArgs a{};
-    a.in = d_in;
-    a.out = d_out;
-    a.n = n;
-    a.num_tiles = static_cast<uint32_t>((n + p->tile_elems - 1) / p->tile_elems);
-    a.hdr = p->hdr16;
-    a.desc = p->desc16;
-    a.wait_budget_ns = p->wait_budget_ns;
     if ((reinterpret_cast<uintptr_t>(p->desc16) & 15u) != 0)
         return fail(GPS_ERR_CUDA, "internal: misaligned descriptor region");
-    const gps::SegArgs sg{d_offsets, static_cast<uint32_t>(num_segments)};
-    const cudaError_t err = launch_generic(p->dtype, kind == GPS_SCAN_INCLUSIVE, a, &sg, p->num_sms,
-                                           reinterpret_cast<cudaStream_t>(stream), &p->last_launch);
+    *a = gps::ScanArgs{};
+    a->in = d_in;
+    a->out = d_out;
+    a->n = n;
+    a->num_tiles = static_cast<uint32_t>((n + p->tile_elems - 1) / p->tile_elems);
+    a->hdr = p->hdr16;
+    a->desc = p->desc16;
+    a->wait_budget_ns = p->wait_budget_ns;
+    *sg = gps::SegArgs{d_offsets, static_cast<uint32_t>(num_segments)};
+    return GPS_OK;
+}
+
+}  // namespace
+
+gps_status gps_scan_segmented(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                              const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream) {
+    if (d_offsets == nullptr && n != 0) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL offsets");
+    gps::ScanArgs a;
+    gps::SegArgs sg;
+    gps_status st = prepare_generic(p, kind, d_in, d_out, n, d_offsets, num_segments, &a, &sg);
+    if (st != GPS_OK || n == 0) return st;
+    const cudaError_t err = launch_generic(p->dtype, kind == GPS_SCAN_INCLUSIVE, a, &sg, generic_config(p, true, n),
+                                           p->num_sms, reinterpret_cast<cudaStream_t>(stream), &p->last_launch);
     if (err != cudaSuccess) return cuda_fail(err, "batched scan launch");
+    return GPS_OK;
+}
+
+gps_status gps_plan_autotune(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                             const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream,
+                             uint32_t* out_unit, uint32_t* out_ctas) {
+    gps::ScanArgs a;
+    gps::SegArgs sg;
+    gps_status st = prepare_generic(p, kind, d_in, d_out, n, d_offsets, num_segments, &a, &sg);
+    if (st != GPS_OK) return st;
+    if (n == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "nothing to tune for n == 0");
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t err = cudaStreamIsCapturing(s, &cap);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaStreamIsCapturing");
+    if (cap != cudaStreamCaptureStatusNone) return fail(GPS_ERR_INVALID_ARGUMENT, "autotuning cannot be captured");
+    const bool seg = d_offsets != nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    int best = -1;
+    float best_ms = 0.0f;
+    for (int c = 0; c < gps::kNumGenericCandidates && err == cudaSuccess; ++c) {
+        const gps::GenericConfig& cfg = gps::kGenericCandidates[c];
+        gps::LaunchInfo info{};
+        const gps::SegArgs* sgp = seg ? &sg : nullptr;
+        const bool incl = kind == GPS_SCAN_INCLUSIVE;
+        err = launch_generic(p->dtype, incl, a, sgp, cfg, p->num_sms, s, &info);  // warm-up
+        if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+        for (int r = 0; r < 3 && err == cudaSuccess; ++r)
+            err = launch_generic(p->dtype, incl, a, sgp, cfg, p->num_sms, s, &info);
+        if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        if (err == cudaSuccess && (best < 0 || ms < best_ms)) {
+            best = c;
+            best_ms = ms;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (err != cudaSuccess) return cuda_fail(err, "autotuning");
+    p->tuned[seg ? 1 : 0][size_class(n)] = static_cast<int8_t>(best);
+    if (out_unit) *out_unit = gps::kGenericCandidates[best].unit;
+    if (out_ctas) *out_ctas = gps::kGenericCandidates[best].ctas_div;
+    return gps_plan_check(p, stream);
+}
+
+gps_status gps_plan_set_generic_config(gps_plan p, int segmented, uint64_t n, uint32_t unit, uint32_t ctas_div) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    for (int c = 0; c < gps::kNumGenericCandidates; ++c) {
+        if (gps::kGenericCandidates[c].unit == unit && gps::kGenericCandidates[c].ctas_div == ctas_div) {
+            p->tuned[segmented ? 1 : 0][size_class(n)] = static_cast<int8_t>(c);
+            return GPS_OK;
+        }
+    }
+    return fail(GPS_ERR_INVALID_ARGUMENT, "no launch configuration with %u tiles per unit and CTA divisor %u", unit,
+                ctas_div);
+}
+
+gps_status gps_plan_generic_config(gps_plan p, int segmented, uint64_t n, uint32_t* out_unit, uint32_t* out_ctas_div,
+                                   int* out_tuned) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    const gps::GenericConfig cfg = generic_config(p, segmented != 0, n);
+    if (out_unit) *out_unit = cfg.unit;
+    if (out_ctas_div) *out_ctas_div = cfg.ctas_div;
+    if (out_tuned) *out_tuned = p->tuned[segmented ? 1 : 0][size_class(n)] >= 0 ? 1 : 0;
     return GPS_OK;
 }
 

@@ -113,16 +113,29 @@ cudaError_t launch_csdl(gps_dtype dtype, bool inclusive, bool stall_mode, const 
                         int num_sms, cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_rts(gps_dtype dtype, bool inclusive, const ScanArgs& a, void* tile_sums,
                        int num_sms, cudaStream_t stream, LaunchInfo* info);
+// Launch configuration of the generic kernel: tiles per lookback unit (1 or
+// 4; the unit is what one CTA takes from the work counter) and the CTA count
+// as a fraction of the resident maximum (1 = all, 2 = half).
+struct GenericConfig {
+    uint32_t unit;
+    uint32_t ctas_div;
+};
+constexpr GenericConfig kGenericCandidates[] = {{4, 1}, {1, 1}, {4, 2}, {1, 2}};
+constexpr int kNumGenericCandidates = 4;
+// Untuned choice: units of 4 tiles once there are at least two such units
+// per SM, else single-tile units (more CTAs busy on small inputs).
+GenericConfig default_generic_config(uint64_t n, uint32_t tile_elems, int num_sms);
+
 // Generic single-pass scan (scan_seg.cuh), one per scan operation; `sg` null
 // for a plain scan. Buffers must be 16-byte aligned; descriptors are 16 bytes.
-cudaError_t launch_seg_u32(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
-                           LaunchInfo* info);
-cudaError_t launch_seg_u64(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
-                           LaunchInfo* info);
-cudaError_t launch_seg_f32(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
-                           LaunchInfo* info);
-cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
-                            LaunchInfo* info);
+cudaError_t launch_seg_u32(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg, int num_sms,
+                           cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_u64(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg, int num_sms,
+                           cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_f32(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg, int num_sms,
+                           cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                            int num_sms, cudaStream_t stream, LaunchInfo* info);
 
 uint32_t csdl_tile_elems(gps_dtype dtype);
 // Sets the text gps_last_error() returns on this host thread.

@@ -2,8 +2,8 @@
 #include "seg_launch.cuh"
 
 namespace gps {
-cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, int num_sms, cudaStream_t stream,
-                          LaunchInfo* info) {
-    return launch_seg_op<OpF32C>(inclusive, a, sg, num_sms, stream, info);
+cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg, int num_sms,
+                          cudaStream_t stream, LaunchInfo* info) {
+    return launch_seg_op<OpF32C>(inclusive, a, sg, cfg, num_sms, stream, info);
 }
 }  // namespace gps

@@ -129,6 +129,33 @@ gps_status gps_scan(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d
 gps_status gps_scan_segmented(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
                               const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream);
 
+/* Autotuner of the batched / floating-point kernel. Times each launch
+ * configuration it knows -- tiles per lookback unit (1 or 4 tiles of 4096
+ * 4-byte or 2048 8-byte elements) times CTA count (one per SM, or half) -- on
+ * these buffers (same arguments as gps_scan_segmented; d_offsets NULL for a
+ * plain scan of a floating-point plan), and keeps the fastest for every later
+ * scan of this plan of the same kind (batched or plain) whose n is in the
+ * same size class (n within a factor of four). Without tuning a size class
+ * uses units of 4 tiles once there are two such units per SM, else 1 tile.
+ * d_out is overwritten (with a correct result). Synchronizes `stream`; not
+ * allowed while the stream is being captured. The chosen configuration is
+ * returned in out_unit / out_ctas_div (either may be NULL).
+ * No counterpart in the reference: its tile shape and grid are compile-time
+ * constants (ChainedScanDecoupledLookbackDispatcher.cuh:13-18). */
+gps_status gps_plan_autotune(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
+                             const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream,
+                             uint32_t* out_unit, uint32_t* out_ctas_div);
+
+/* Launch configuration a batched (segmented != 0) or plain generic-kernel
+ * scan of n elements would use now: tiles per unit, CTA divisor (1: one CTA
+ * per SM, 2: half), and whether it comes from gps_plan_autotune(). */
+gps_status gps_plan_generic_config(gps_plan plan, int segmented, uint64_t n, uint32_t* out_unit,
+                                   uint32_t* out_ctas_div, int* out_tuned);
+
+/* Sets the launch configuration of a size class by hand (to restore a saved
+ * tuning, or to test one configuration): unit 1 or 4, ctas_div 1 or 2. */
+gps_status gps_plan_set_generic_config(gps_plan plan, int segmented, uint64_t n, uint32_t unit, uint32_t ctas_div);
+
 /* Scan of a host array: copies h_in to the device, scans, copies the result
  * to h_out, in chunks so that the copies in both directions overlap the
  * scans; returns when h_out is complete (synchronizes `stream`). Host buffers

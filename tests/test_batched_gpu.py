@@ -142,6 +142,46 @@ def test_segmented_and_plain_scans_share_a_u32_plan(cuda, max_n):
             assert np.array_equal(full.cpu().numpy().view(np.uint32), want)
 
 
+@pytest.mark.parametrize("unit,ctas_div", [(1, 1), (4, 1), (1, 2), (4, 2)])
+def test_every_launch_configuration_is_exact(cuda, unit, ctas_div):
+    lengths = config3_lengths(seed=11)[:600]
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    rng = np.random.default_rng(unit * 10 + ctas_div)
+    x = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    xf = fp_input("normal", n, seed=5)
+    with Plan("csdl", "u32", max_n=n) as plan, Plan("csdl", "f32c", max_n=n) as fplan:
+        plan.set_generic_config(n, unit, ctas_div)
+        fplan.set_generic_config(n, unit, ctas_div, segmented=False)
+        assert plan.generic_config(n) == {"unit_tiles": unit, "ctas_div": ctas_div, "tuned": True}
+        for inclusive in (False, True):
+            got = plan.scan_segmented(dev(x), d_off, inclusive=inclusive)
+            plan.check()
+            assert np.array_equal(got.cpu().numpy().view(np.uint32), oracle.segscan(x, offs, inclusive))
+        got = fplan.scan(torch.from_numpy(xf).cuda(), inclusive=True).cpu().numpy()
+        fplan.check()
+        assert fp_errors(got, oracle.scan_f32_exact(xf, inclusive=True), xf)[0] <= 1e-6
+
+
+def test_autotune_keeps_a_configuration_per_size_class(cuda):
+    lengths = config3_lengths(seed=12)[:1000]
+    offs = offsets_of(lengths)
+    n = int(offs[-1])
+    rng = np.random.default_rng(12)
+    x = rng.integers(0, 256, size=n, dtype=np.uint32)
+    d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+    with Plan("csdl", "u32", max_n=n) as plan:
+        assert not plan.generic_config(n)["tuned"]
+        choice = plan.autotune(dev(x), d_off)
+        cfg = plan.generic_config(n)
+        assert cfg["tuned"] and (cfg["unit_tiles"], cfg["ctas_div"]) == (choice["unit_tiles"], choice["ctas_div"])
+        assert not plan.generic_config(n // 16)["tuned"]  # another size class
+        got = plan.scan_segmented(dev(x), d_off)
+        plan.check()
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), oracle.segscan(x, offs, False))
+
+
 # ------------------------------------------------------------ floating point
 def fp_errors(got, exact, x):
     got = got.astype(np.float64)
