@@ -49,7 +49,7 @@ import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "csdl_u32_exclusive_2pow26_ncu_full.txt")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "scan_l2_kernel_u32_exclusive_2pow28.md")
 METRIC = "scan GB/s (u32 exclusive, n=2^28, chained scan), % of D2D-copy roofline"
 
 

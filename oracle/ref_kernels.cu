@@ -10,7 +10,6 @@
 // The tests look the kernels up by name in the loaded module and launch them
 // exactly as the reference dispatchers do.
 #include "ChainedScanDecoupledLookback.cuh"
-#include "EmulatedDeadlocking.cuh"
 #include "ReduceThenScan.cuh"
 #include "UtilityKernels.cuh"
 
@@ -22,5 +21,4 @@ template __global__ void ReduceThenScan::Reduce<8, 4>(uint32_t*, uint32_t*, cons
 template __global__ void ReduceThenScan::SpineScan<32, 4>(uint32_t*, const uint32_t);
 template __global__ void ReduceThenScan::PropagateInclusive<8, 4>(uint32_t*, uint32_t*, const uint32_t);
 template __global__ void ReduceThenScan::PropagateExclusive<8, 4>(uint32_t*, uint32_t*, const uint32_t);
-template __global__ void EmulatedDeadlocking::EmulatedDeadlock<8, 4>(uint32_t*, volatile uint32_t*,
-                                                                    volatile uint32_t*, const uint32_t);
+

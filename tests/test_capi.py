@@ -73,3 +73,28 @@ def test_plan_create_rejects_bad_arguments_before_any_cuda_call():
 def test_compat_selftest_was_built():
     from gpuprefixsums_gb300.build import SELFTEST_BIN
     assert os.access(SELFTEST_BIN, os.X_OK)
+
+
+REFERENCE_DRIVER = os.path.join(os.environ.get("GPS_REFERENCE_DIR", "/root/reference/GPUPrefixSumsCUDA"),
+                                "GPUPrefixSumsCUDA.cu")
+
+
+@pytest.mark.skipif(not os.path.exists(REFERENCE_DRIVER), reason="reference checkout not present")
+def test_reference_driver_builds_unchanged_against_the_compat_headers(tmp_path):
+    """The reference's own main() (GPUPrefixSumsCUDA.cu:14-38) compiles and
+    links against include/gps_compat/ and libgps.so with no edit: its quoted
+    includes resolve to the compat headers once the file is compiled from a
+    directory without the reference headers beside it."""
+    import shutil
+    import subprocess
+
+    from gpuprefixsums_gb300 import build as B
+    src = tmp_path / "GPUPrefixSumsCUDA.cu"
+    shutil.copyfile(REFERENCE_DRIVER, src)
+    exe = tmp_path / "driver"
+    cmd = [B.nvcc_path(), *B.ARCH_FLAGS, "-std=c++17", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "include", "gps_compat"), "-o", str(exe), str(src),
+           "-L", B.PKG_DIR, "-lgps", "-Xlinker", "-rpath", "-Xlinker", B.PKG_DIR]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert exe.exists()
