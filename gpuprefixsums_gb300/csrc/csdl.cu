@@ -43,16 +43,20 @@ cudaError_t launch_csdl_t(const ScanArgs& a, int num_sms, cudaStream_t stream, L
 // (152 x 6 x 64 KB at most): measured on GB300 at 2^28 elements, 6 units
 // beat both 4-5 (too shallow to cover the lookback) and 7-8 (the re-loads
 // start missing in L2).
+// u64 keeps 4 reduce-pass stages: its per-thread prefixes take twice the
+// shared memory.
 constexpr int kL2Warps = 4;
-constexpr int kL2RStages = 5;
+template <typename T>
+constexpr int kL2RStages = sizeof(T) == 8 ? 4 : 5;
 constexpr int kL2SStages = 8;
 constexpr int kL2Queue = 6;
 constexpr int kL2Unit = 4;
 
 template <typename T, bool INCL, bool STALL>
 cudaError_t launch_l2_t(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
-    auto kern = scan_l2_kernel<T, kL2Warps, kL2RStages, kL2SStages, kL2Queue, kL2Unit, INCL, STALL>;
-    constexpr size_t smem = l2_smem_bytes<T, kL2Warps, kL2RStages, kL2SStages, kL2Queue>();
+    auto kern = scan_l2_kernel<T, kL2Warps, kL2RStages<T>, kL2SStages, kL2Queue, kL2Unit, INCL, STALL>;
+    constexpr size_t smem = l2_smem_bytes<T, kL2Warps, kL2RStages<T>, kL2SStages, kL2Queue, kL2Unit>();
+    static_assert(smem <= 232448, "227 KB of shared memory per CTA");
     constexpr int threads = L2Shape<T, kL2Warps>::kThreads;
     int occ = 0;
     cudaError_t err = resident_ctas_per_sm(kern, threads, smem, &occ);

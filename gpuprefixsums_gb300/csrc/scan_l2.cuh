@@ -30,7 +30,7 @@
 
 namespace gps {
 
-template <typename T, int RW, int RS, int SS, int Q>
+template <typename T, int RW, int RS, int SS, int Q, int G>
 struct L2Ctrl {
     uint64_t rfull[RS];     // R-loader -> reduce: tile landed
     uint64_t rfree[RS];     // reduce -> R-loader: stage read
@@ -47,13 +47,16 @@ struct L2Ctrl {
     uint32_t end_seq;       // first unit sequence number the reduce warps did not take
     T uagg[Q];
     T upre[Q];
-    T r_warp_tot[2][RW];
-    T f_warp_tot[2][RW];
+    T r_warp_tot[2][RW];  // inclusive warp totals of the reduce pass
+    // Exclusive prefix of each reduce/finalize thread's 128 bytes within its
+    // unit, from the reduce pass: the scan pass then needs no cross-warp
+    // exchange (no warp scan, no barrier) per tile.
+    T tpre[Q][G][RW * 32];
 };
 
-template <typename T, int RW, int RS, int SS, int Q>
+template <typename T, int RW, int RS, int SS, int Q, int G>
 constexpr size_t l2_smem_bytes() {
-    return static_cast<size_t>(RS + SS) * TileShape<T, RW>::kTile * sizeof(T) + sizeof(L2Ctrl<T, RW, RS, SS, Q>);
+    return static_cast<size_t>(RS + SS) * TileShape<T, RW>::kTile * sizeof(T) + sizeof(L2Ctrl<T, RW, RS, SS, Q, G>);
 }
 
 template <typename T, int RW>
@@ -76,7 +79,7 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
     static_assert(Q > LW, "every lookback warp needs its own queue entry");
     using D = DescTraits<T>;
     using word = typename D::word;
-    using Ctrl = L2Ctrl<T, RW, RS, SS, Q>;
+    using Ctrl = L2Ctrl<T, RW, RS, SS, Q, G>;
 
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     T* rbuf = reinterpret_cast<T*>(smem_raw);
@@ -382,8 +385,8 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                         total += static_cast<const T*>(a.in)[gbase + li];
                 }
             }
-            total = warp_sum(total);
-            if (lane == 0) ctrl->r_warp_tot[rn & 1u][rw] = total;
+            const T winc = warp_inclusive_scan(total, lane);
+            if (lane == 31) ctrl->r_warp_tot[rn & 1u][rw] = winc;
             const bool stop = named_bar_or(1, NROLE, !live);
             // The stage has been read by every reduce thread.
             if (lane == 0 && live) ptx::mbar_arrive(&ctrl->rfree[s]);
@@ -394,11 +397,19 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                 }
                 break;
             }
-            if (r == 0) {
-                T agg = 0;
+            {
+                // This thread's prefix within the unit, for the scan pass.
+                T wpre = 0, agg = 0;
 #pragma unroll
-                for (int w2 = 0; w2 < RW; ++w2) agg += ctrl->r_warp_tot[rn & 1u][w2];
+                for (int w2 = 0; w2 < RW; ++w2) {
+                    const T x = ctrl->r_warp_tot[rn & 1u][w2];
+                    wpre += (static_cast<uint32_t>(w2) < rw) ? x : T(0);
+                    agg += x;
+                }
+                ctrl->tpre[(rn / G) % Q][rn % G][r] = unit_agg + wpre + (winc - total);
                 unit_agg += agg;
+            }
+            if (r == 0) {
                 if ((t % G) == G - 1) {
                     const uint32_t u = t / G;
                     const int q = static_cast<int>((rn / G) % Q);
@@ -427,15 +438,14 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                                                   : D::pack(kAggregate, epoch, unit_agg));
                     ctrl->uagg[q] = unit_agg;
                     ptx::mbar_arrive(&ctrl->ureduced[q]);
-                    unit_agg = 0;
                 }
             }
+            if ((rn % G) == G - 1) unit_agg = 0;
         }
     }
     // ======================================================== finalize
     else {
         const uint32_t f = tid - kWarpFinal * 32;
-        const uint32_t fw = warp - kWarpFinal;
         const uint32_t rot = f & 7u;
         T run = 0;
         bool go = true;
@@ -443,8 +453,9 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
             const int s = static_cast<int>(sn % SS);
             const uint32_t i = sn / G;  // unit sequence number
             const int q = static_cast<int>(i % Q);
-            const bool ok = ptx::mbar_try_wait(&ctrl->sfull[s], (sn / SS) & 1u) ||
-                            ptx::mbar_wait_bounded(&ctrl->sfull[s], (sn / SS) & 1u, ptx::global_timer_ns() + long_budget);
+            const bool ok = __all_sync(kFullMask, ptx::mbar_try_wait(&ctrl->sfull[s], (sn / SS) & 1u) ||
+                                                      ptx::mbar_wait_bounded(&ctrl->sfull[s], (sn / SS) & 1u,
+                                                                             ptx::global_timer_ns() + long_budget));
             const uint32_t t = ok ? ctrl->s_tile[s] : kTileEnd;
             const bool live = t != kTileEnd;
             T* sb = sbuf + static_cast<size_t>(s) * TILE;
@@ -474,6 +485,12 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                     v[e] = x;
                 }
             }
+            if (!live) {
+                if (!ok && f == 0) raise_error(a.hdr, kErrPipelineTimeout);
+                if (lane == 0) ptx::mbar_arrive(&ctrl->sdone[s]);  // lets the storer see the end
+                go = false;
+                break;
+            }
             T cs[CHUNKS];
 #pragma unroll
             for (int c8 = 0; c8 < CHUNKS; ++c8) {
@@ -485,14 +502,6 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
             T cpre[CHUNKS];
             T total;
             rotated_chunk_prefix<T, CHUNKS>(cs, full_tile ? rot : 0u, cpre, total);
-            const T winc = warp_inclusive_scan(total, lane);
-            if (lane == 31) ctrl->f_warp_tot[sn & 1u][fw] = winc;
-            if (named_bar_or(2, NROLE, !live)) {
-                if (!ok && f == 0) raise_error(a.hdr, kErrPipelineTimeout);
-                if (lane == 0) ptx::mbar_arrive(&ctrl->sdone[s]);  // lets the storer see the end
-                go = false;
-                break;
-            }
             if ((sn % G) == 0) {
                 // First tile of a unit: wait for the unit's prefix.
                 bool pok = ptx::mbar_try_wait(&ctrl->uprefix[q], (i / Q) & 1u) ||
@@ -501,15 +510,8 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                 if (!pok && lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
                 run = ctrl->upre[q];
             }
-            T wpre = 0, agg = 0;
-#pragma unroll
-            for (int w2 = 0; w2 < RW; ++w2) {
-                const T x = ctrl->f_warp_tot[sn & 1u][w2];
-                wpre += (static_cast<uint32_t>(w2) < fw) ? x : T(0);
-                agg += x;
-            }
-            const T base = run + wpre + (winc - total);
-            run += agg;
+            // The reduce pass left this thread's prefix within the unit.
+            const T base = run + ctrl->tpre[q][sn % G][f];
 #pragma unroll
             for (int c8 = 0; c8 < CHUNKS; ++c8) {
                 T acc = base + cpre[c8];
