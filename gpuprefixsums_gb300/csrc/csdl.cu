@@ -37,18 +37,18 @@ cudaError_t launch_csdl_t(const ScanArgs& a, int num_sms, cudaStream_t stream, L
 }
 
 // L2-buffered kernel (16-byte-aligned buffers): 4 reduce + 4 finalize warps
-// over 16 KB tiles, 5 reduce-pass and 8 scan-pass stages (208 KB, one CTA per
-// SM), lookback units of 4 tiles (64 KB), 6 units in flight per CTA. The
-// queue depth sets how much input waits in L2 between the two passes
-// (152 x 6 x 64 KB at most): measured on GB300 at 2^28 elements, 6 units
-// beat both 4-5 (too shallow to cover the lookback) and 7-8 (the re-loads
-// start missing in L2).
-// u64 keeps 4 reduce-pass stages: its per-thread prefixes take twice the
-// shared memory.
+// over 16 KB tiles, lookback units of 4 tiles (64 KB), 6 units in flight per
+// CTA, one CTA per SM. Each unit is prefetched into L2 when its id is taken,
+// so the reduce-pass ring needs few stages: 4 reduce-pass and 9 scan-pass
+// stages (208 KB; 3 + 9 for u64, whose per-thread prefixes take twice the
+// room). Measured on GB300 at 2^28 u32 elements: 4 + 9 stages beat 5 + 8 by
+// 4% once the prefetch was in (3 + 10 starves the reduce pass), and 6 units
+// in flight beat 4, 5 and 7 (the queue depth sets how much input waits in L2
+// between the two passes, 152 x 6 x 64 KB at most).
 constexpr int kL2Warps = 4;
 template <typename T>
-constexpr int kL2RStages = sizeof(T) == 8 ? 4 : 5;
-constexpr int kL2SStages = 8;
+constexpr int kL2RStages = sizeof(T) == 8 ? 3 : 4;
+constexpr int kL2SStages = 9;
 constexpr int kL2Queue = 6;
 constexpr int kL2Unit = 4;
 

@@ -117,6 +117,14 @@ __device__ __forceinline__ void bulk_load_hint(void* smem_dst, const void* gmem_
         : "memory");
 }
 
+// Prefetch of global memory into L2 (no shared memory, no completion
+// signal), with an L2 cache policy. Address and size 16-byte aligned.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* gmem_src, uint32_t bytes, uint64_t policy) {
+    asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(gmem_src), "r"(bytes),
+                 "l"(policy)
+                 : "memory");
+}
+
 // shared -> global with an L2 cache policy, tracked as a bulk async-group.
 __device__ __forceinline__ void bulk_store_hint(void* gmem_dst, const void* smem_src, uint32_t bytes,
                                                 uint64_t policy) {

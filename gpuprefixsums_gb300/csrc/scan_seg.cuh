@@ -398,15 +398,24 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                 return static_cast<uint32_t>(raw);
             };
             uint32_t rn = 0;
-            uint64_t upcoming = acquire();
             bool ok = true;
             for (uint32_t i = 0; ok; ++i) {
                 const int q = static_cast<int>(i % Q);
                 if (i >= Q && !wait1(&ctrl->ufree[q], ((i - Q) / Q) & 1u, long_budget)) break;
-                const uint32_t u = resolve(upcoming);
-                upcoming = acquire();
+                // Take the unit id now and start its HBM reads into L2 (see
+                // scan_l2.cuh): the stage loads below then hit L2.
+                const uint32_t u = resolve(acquire());
                 ctrl->unit_of[q] = u;
                 ptx::mbar_arrive(&ctrl->uknown[q]);
+                if (u != kTileEnd) {
+#pragma unroll
+                    for (int k = 0; k < G; ++k) {
+                        const uint32_t bb = bulk_bytes_of(u * G + k);
+                        if (bb)
+                            ptx::bulk_prefetch_l2(static_cast<const T*>(a.in) + static_cast<uint64_t>(u * G + k) * TILE,
+                                                  bb, pol);
+                    }
+                }
                 if (u == kTileEnd) {
                     for (uint32_t m = 1; m < LW && ok; ++m) {
                         const uint32_t i2 = i + m;
