@@ -402,20 +402,13 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
             for (uint32_t i = 0; ok; ++i) {
                 const int q = static_cast<int>(i % Q);
                 if (i >= Q && !wait1(&ctrl->ufree[q], ((i - Q) / Q) & 1u, long_budget)) break;
-                // Take the unit id now and start its HBM reads into L2 (see
-                // scan_l2.cuh): the stage loads below then hit L2.
+                // The unit id is taken only now, when its loads follow (see
+                // scan_l2.cuh). No L2 prefetch here: this kernel is bound by
+                // its per-tile work, and the prefetched lines only crowd the
+                // L2 (measured: 7% slower on the 4096-segment batch).
                 const uint32_t u = resolve(acquire());
                 ctrl->unit_of[q] = u;
                 ptx::mbar_arrive(&ctrl->uknown[q]);
-                if (u != kTileEnd) {
-#pragma unroll
-                    for (int k = 0; k < G; ++k) {
-                        const uint32_t bb = bulk_bytes_of(u * G + k);
-                        if (bb)
-                            ptx::bulk_prefetch_l2(static_cast<const T*>(a.in) + static_cast<uint64_t>(u * G + k) * TILE,
-                                                  bb, pol);
-                    }
-                }
                 if (u == kTileEnd) {
                     for (uint32_t m = 1; m < LW && ok; ++m) {
                         const uint32_t i2 = i + m;

@@ -7,13 +7,13 @@
 
 namespace gps {
 
-// 4 reduce + 4 finalize warps over 16 KB tiles, 5 reduce-pass and 8
-// scan-pass stages, 6 units in flight per CTA (the measured optimum of the
-// u32 L2-buffered kernel, scan_l2.cuh). The unit (1 or 4 tiles) and the CTA
-// count come from the plan's launch configuration (GenericConfig).
+// 4 reduce + 4 finalize warps over 16 KB tiles, 4 reduce-pass and 9
+// scan-pass stages, 6 units in flight per CTA (measured on GB300: 4 + 9
+// beats 5 + 8 by 3-8% on the batched workloads). The unit (1 or 4 tiles) and
+// the CTA count come from the plan's launch configuration (GenericConfig).
 constexpr int kSegWarps = 4;
-constexpr int kSegRStages = 5;
-constexpr int kSegSStages = 8;
+constexpr int kSegRStages = 4;
+constexpr int kSegSStages = 9;
 constexpr int kSegQueue = 6;
 
 template <class Op, bool INCL, bool SEG, int UNIT>
