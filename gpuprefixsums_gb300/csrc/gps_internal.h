@@ -4,6 +4,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "gps.h"
@@ -113,6 +114,17 @@ cudaError_t launch_csdl(gps_dtype dtype, bool inclusive, bool stall_mode, const 
                         int num_sms, cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_rts(gps_dtype dtype, bool inclusive, const ScanArgs& a, void* tile_sums,
                        int num_sms, cudaStream_t stream, LaunchInfo* info);
+// Tensor maps of the generic kernel: the buffer seen as rows of 128 bytes
+// (32 four-byte or 16 eight-byte elements), boxes of 128 rows (one 16 KB
+// tile), 128-byte swizzle. Rows past the last full row are the kernel's to
+// handle with plain loads and stores. Host-side; encodes through the driver
+// entry point cuTensorMapEncodeTiled.
+struct RowMaps {
+    CUtensorMap in;
+    CUtensorMap out;
+};
+cudaError_t encode_row_maps(const void* in, void* out, uint64_t n, uint32_t elem_size, RowMaps* maps);
+
 // Launch configuration of the generic kernel: tiles per lookback unit (1 or
 // 4; the unit is what one CTA takes from the work counter) and the CTA count
 // as a fraction of the resident maximum (1 = all, 2 = half).

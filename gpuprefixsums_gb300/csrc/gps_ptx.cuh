@@ -125,6 +125,30 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void* gmem_src, uint32_t 
                  : "memory");
 }
 
+// Tiled tensor copies (TMA) of a 2-D tensor map passed as a __grid_constant__
+// kernel parameter. x is the innermost coordinate (always 0 here: whole
+// 128-byte rows), y the row.
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, int32_t x, int32_t y, uint64_t* bar,
+                                            uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_addr(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_addr(bar)), "l"(policy)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(const void* tmap, int32_t x, int32_t y, const void* smem_src,
+                                             uint64_t policy) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%1, %2}], [%3], %4;" ::"l"(
+                     reinterpret_cast<uint64_t>(tmap)),
+                 "r"(x), "r"(y), "r"(smem_addr(smem_src)), "l"(policy)
+                 : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tensormap(const void* tmap) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
+}
+
 // shared -> global with an L2 cache policy, tracked as a bulk async-group.
 __device__ __forceinline__ void bulk_store_hint(void* gmem_dst, const void* smem_src, uint32_t bytes,
                                                 uint64_t policy) {

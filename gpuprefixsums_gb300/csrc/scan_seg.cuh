@@ -38,23 +38,6 @@ __device__ __forceinline__ ptx::u64x2 seg_pack(uint32_t status, bool flag, uint3
     return w;
 }
 
-// Rotates 16-byte chunks within a thread's items: v'[c] = v[(c - amount) & 7].
-template <typename T, int CHUNKS, int EPC>
-__device__ __forceinline__ void rotate_chunks(T (&v)[CHUNKS * EPC], uint32_t amount) {
-#pragma unroll
-    for (int b = 1; b < CHUNKS; b <<= 1) {
-        if (amount & b) {
-            T t[CHUNKS * EPC];
-#pragma unroll
-            for (int x = 0; x < CHUNKS * EPC; ++x) t[x] = v[x];
-#pragma unroll
-            for (int c = 0; c < CHUNKS; ++c)
-#pragma unroll
-                for (int e = 0; e < EPC; ++e) v[c * EPC + e] = t[((c - b) & (CHUNKS - 1)) * EPC + e];
-        }
-    }
-}
-
 // Segmented combine of (a, fa) followed by (b, fb).
 template <class Op>
 __device__ __forceinline__ void seg_combine(typename Op::S& a, bool& fa, typename Op::S b, bool fb) {
@@ -67,42 +50,6 @@ __device__ __forceinline__ typename Op::C chain_warp_sum(typename Op::C x) {
 #pragma unroll
     for (int m = 16; m; m >>= 1) x = Op::chain_add(x, Op::chain_shfl_xor(x, m));
     return x;
-}
-
-// Per-thread work on a thread's CHUNKS x EPC items. Register chunk c holds
-// logical chunk (c + rrot) & (CHUNKS - 1) (the bank-conflict-free read order;
-// rrot = 0 when the items were read in logical order). hb holds the items'
-// head bits in logical order. Each chunk is summed by its own chain of EPC
-// items, so a thread runs CHUNKS short independent chains instead of one long
-// one; only the CHUNKS chunk aggregates are then put in logical order.
-template <class Op, int CHUNKS, int EPC, bool SEG>
-__device__ __forceinline__ uint32_t chunk_head_bits(uint32_t hb, uint32_t c, uint32_t rrot) {
-    if (!SEG) return 0u;
-    const uint32_t l = (c + rrot) & (CHUNKS - 1);
-    return (hb >> (l * EPC)) & ((1u << EPC) - 1u);
-}
-
-// Chunk aggregates in logical order; returns the mask (logical order) of the
-// chunks that hold a segment head.
-template <class Op, int CHUNKS, int EPC, bool SEG, bool REORDER>
-__device__ __forceinline__ uint32_t chunk_aggregates(const typename Op::T (&v)[CHUNKS * EPC], uint32_t hb,
-                                                     uint32_t rrot, typename Op::S (&ca)[CHUNKS]) {
-    using S = typename Op::S;
-    uint32_t mask = 0;
-#pragma unroll
-    for (int c = 0; c < CHUNKS; ++c) {
-        const uint32_t bits = chunk_head_bits<Op, CHUNKS, EPC, SEG>(hb, c, rrot);
-        S x = Op::zero();
-#pragma unroll
-        for (int e = 0; e < EPC; ++e) x = ((bits >> e) & 1u) ? Op::lift(v[c * EPC + e]) : Op::acc(x, v[c * EPC + e]);
-        ca[c] = x;
-        mask |= (bits != 0u ? 1u : 0u) << c;
-    }
-    if (REORDER) {
-        rotate_chunks<S, CHUNKS, 1>(ca, rrot);
-        mask = ((mask << rrot) | (mask >> ((CHUNKS - rrot) & (CHUNKS - 1)))) & ((1u << CHUNKS) - 1u);
-    }
-    return mask;
 }
 
 // Inclusive warp scan of (state, head flag) in lane order. Without FLAGS the
@@ -124,60 +71,26 @@ __device__ __forceinline__ void warp_scan_incl(typename Op::S& s, bool& f, uint3
     }
 }
 
-// Sum of a warp's states in every lane, in no particular order (wrapping
-// integer sums only).
-template <class Op>
-__device__ __forceinline__ typename Op::S warp_sum_unordered(typename Op::S s) {
+// Aggregate of a thread's items in logical order; hb holds their head bits
+// (HEADS = false: no item of the warp is a segment head). One chain, whose
+// step is one add (one FP32 add on hi and one on lo for the compensated
+// scan, see scan_ops.cuh).
+template <class Op, int ITEMS, bool HEADS>
+__device__ __forceinline__ typename Op::S thread_aggregate(const typename Op::T (&v)[ITEMS], uint32_t hb) {
+    typename Op::S x = Op::zero();
 #pragma unroll
-    for (int m = 16; m; m >>= 1) s = Op::combine(s, Op::shfl(s, (threadIdx.x & 31u) ^ static_cast<uint32_t>(m)));
-    return s;
+    for (int e = 0; e < ITEMS; ++e) x = (HEADS && ((hb >> e) & 1u)) ? Op::lift(v[e]) : Op::acc(x, v[e]);
+    return Op::norm(x);
 }
 
-// Thread aggregate of a thread's items and the warp's inclusive scan of it;
-// HEADS = false when no item of the warp is a segment head. UNORDERED: only
-// the warp total is wanted and the type's sums need no order.
-template <class Op, int CHUNKS, int EPC, bool HEADS, bool REORDER, bool UNORDERED>
-__device__ __forceinline__ uint32_t thread_and_warp_scan(const typename Op::T (&v)[CHUNKS * EPC], uint32_t hb,
-                                                         uint32_t rrot, uint32_t lane, typename Op::S (&ca)[CHUNKS],
-                                                         typename Op::S& ws, bool& wf) {
-    using S = typename Op::S;
-    const uint32_t cmask = chunk_aggregates<Op, CHUNKS, EPC, HEADS, REORDER>(v, hb, rrot, ca);
-    S tv = Op::zero();
-    bool tf = false;
+// Scanned outputs of a thread's items from the state before its first item.
+template <class Op, int ITEMS, bool HEADS, bool INCL>
+__device__ __forceinline__ void thread_outputs(typename Op::T (&v)[ITEMS], typename Op::S st, uint32_t hb) {
 #pragma unroll
-    for (int c = 0; c < CHUNKS; ++c) {
-        if (HEADS)
-            seg_combine<Op>(tv, tf, ca[c], (cmask >> c) & 1u);
-        else
-            tv = Op::combine(tv, ca[c]);
-    }
-    tv = Op::norm(tv);
-    if (UNORDERED && !HEADS) {
-        tv = warp_sum_unordered<Op>(tv);
-    } else {
-        warp_scan_incl<Op, HEADS>(tv, tf, lane);
-    }
-    ws = tv;
-    wf = tf;
-    return cmask;
-}
-
-// Outputs of a thread's items from the state before each chunk (cp, in
-// register order): CHUNKS independent chains of EPC items.
-template <class Op, int CHUNKS, int EPC, bool SEG, bool INCL>
-__device__ __forceinline__ void chunk_outputs(typename Op::T (&v)[CHUNKS * EPC], const typename Op::S (&cp)[CHUNKS],
-                                              uint32_t hb, uint32_t rrot) {
-    using S = typename Op::S;
-#pragma unroll
-    for (int c = 0; c < CHUNKS; ++c) {
-        const uint32_t bits = chunk_head_bits<Op, CHUNKS, EPC, SEG>(hb, c, rrot);
-        S st = cp[c];
-#pragma unroll
-        for (int e = 0; e < EPC; ++e) {
-            const S before = ((bits >> e) & 1u) ? Op::zero() : st;
-            st = Op::acc(before, v[c * EPC + e]);
-            v[c * EPC + e] = INCL ? Op::out(st) : Op::out(before);
-        }
+    for (int e = 0; e < ITEMS; ++e) {
+        const typename Op::S before = (HEADS && ((hb >> e) & 1u)) ? Op::zero() : st;
+        st = Op::acc(before, v[e]);
+        v[e] = INCL ? Op::out(st) : Op::out(before);
     }
 }
 
@@ -286,8 +199,11 @@ struct SegCtrl {
     C upre[Q];
     S r_wtot[2][RW];
     uint32_t r_wflag[2][RW];
-    S f_wtot[2][RW];
-    uint32_t f_wflag[2][RW];
+    // From the reduce pass to the scan pass: the state before each thread's
+    // 128 bytes within its unit, and (bit = lane) whether a segment head lies
+    // between the unit's start and that thread.
+    S tpre[Q][G][RW * 32];
+    uint32_t tflag[Q][G][RW];
     // Segmented scans only (one unused entry otherwise):
     uint32_t heads[SEG ? Q : 1][G][kHeadWords];  // bit b of word w: element 32w+b is a segment head
     uint32_t sample[SEG ? 1024 : 1];             // offsets[j * sample_stride], to start head searches
@@ -306,7 +222,9 @@ struct SegShape {
 };
 
 template <class Op, int RW, int RS, int SS, int Q, int G, bool INCL, bool SEG>
-__global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel(const ScanArgs a, const SegArgs sg) {
+__global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
+    scan_seg_kernel(const ScanArgs a, const SegArgs sg, const __grid_constant__ CUtensorMap tin,
+                    const __grid_constant__ CUtensorMap tout) {
     using T = typename Op::T;
     using S = typename Op::S;
     using C = typename Op::C;
@@ -320,12 +238,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     constexpr uint32_t kWarpLookback = 4, kWarpReduce = 4 + LW, kWarpFinal = 4 + LW + RW;
     constexpr int kHeadWords = TILE / 32;
     static_assert(CHUNKS == 8, "128 bytes per thread");
+    static_assert(NROLE == 128, "a tile is one box of 128 rows of 128 bytes");
     static_assert(Q > LW, "every lookback warp needs its own queue entry");
     using Ctrl = SegCtrl<Op, RW, RS, SS, Q, G, SEG>;
-    // The reduce pass sums the chunk aggregates in logical order for
-    // segmented scans (heads) and for floating point (the summation order of
-    // the scan pass); wrapping integer sums need no order.
-    constexpr bool REORDER = SEG || !std::is_integral<T>::value;
 
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     T* rbuf = reinterpret_cast<T*>(smem_raw);
@@ -336,6 +251,17 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     const uint32_t warp = tid >> 5;
     const uint32_t lane = tid & 31u;
     const uint32_t num_units = (a.num_tiles + G - 1) / G;
+    // The 128-byte swizzle repeats every 1024 bytes: stages must start on a
+    // 1024-byte boundary. (A misaligned window is reported, not used.)
+    if ((ptx::smem_addr(smem_raw) & 1023u) != 0) {
+        if (tid == 0) raise_error(a.hdr, kErrPipelineTimeout);
+        return;
+    }
+    // Rows of 128 bytes: full ones move by TMA; the last, partial row (the
+    // n % ROW tail) by plain loads and stores of its owning thread.
+    constexpr uint32_t ROW = 128 / sizeof(T);
+    const uint64_t rows_full = a.n / ROW;
+    const uint32_t tail = static_cast<uint32_t>(a.n % ROW);
     // Samples of the offsets: every `stride`-th entry, at most 1024.
     const uint32_t nseg = SEG ? sg.num_segments : 0u;
     const uint32_t stride = SEG ? (nseg + 1 + 1023) / 1024 : 1u;
@@ -361,16 +287,54 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
         ctrl->end_seq = 0xFFFFFFFFu;
         ptx::fence_mbar_init();
     }
-    if (SEG)
+    if constexpr (SEG)
         for (uint32_t j = tid; j < nsample; j += blockDim.x) ctrl->sample[j] = sg.offsets[min(j * stride, nseg)];
     __syncthreads();
 
     const uint32_t epoch = ld_volatile_u32(&a.hdr->epoch);
     const uint64_t budget = a.wait_budget_ns;
     const uint64_t long_budget = budget * 4 + 1000000000ull;
-    auto count_of = [&](uint32_t t) -> uint32_t { return t < a.num_tiles ? tile_count<TILE>(a.n, t) : 0u; };
-    auto bulk_bytes_of = [&](uint32_t t) -> uint32_t {
-        return (count_of(t) * static_cast<uint32_t>(sizeof(T))) & ~15u;
+    // Bytes one TMA box brings for tile t (rows past the tensor are filled
+    // with zeros and counted), or 0 when the tile has no full row.
+    auto tma_bytes_of = [&](uint32_t t) -> uint32_t {
+        return (t < a.num_tiles && static_cast<uint64_t>(t) * NROLE < rows_full)
+                   ? static_cast<uint32_t>(TILE * sizeof(T))
+                   : 0u;
+    };
+    // A thread's 128-byte row of tile t, in logical order.
+    auto load_row = [&](const T* stage, uint32_t t, uint32_t thr, T (&v)[ITEMS]) {
+        const uint64_t row = static_cast<uint64_t>(t) * NROLE + thr;
+        if (row < rows_full) {
+            const T* rp = stage + thr * ITEMS;
+#pragma unroll
+            for (int c = 0; c < CHUNKS; ++c) {
+                const Chunk<T> qv = *reinterpret_cast<const Chunk<T>*>(rp + (c ^ static_cast<int>(thr & 7u)) * EPC);
+#pragma unroll
+                for (int e = 0; e < EPC; ++e) v[c * EPC + e] = qv.v[e];
+            }
+        } else {
+            const T* gp = static_cast<const T*>(a.in) + row * ROW;
+#pragma unroll
+            for (int e = 0; e < ITEMS; ++e) v[e] = (row == rows_full && static_cast<uint32_t>(e) < tail) ? gp[e] : T(0);
+        }
+    };
+    auto store_row = [&](T* stage, uint32_t t, uint32_t thr, const T (&v)[ITEMS]) {
+        const uint64_t row = static_cast<uint64_t>(t) * NROLE + thr;
+        if (row < rows_full) {
+            T* rp = stage + thr * ITEMS;
+#pragma unroll
+            for (int c = 0; c < CHUNKS; ++c) {
+                Chunk<T> qv;
+#pragma unroll
+                for (int e = 0; e < EPC; ++e) qv.v[e] = v[c * EPC + e];
+                *reinterpret_cast<Chunk<T>*>(rp + (c ^ static_cast<int>(thr & 7u)) * EPC) = qv;
+            }
+        } else if (row == rows_full) {
+            T* gp = static_cast<T*>(a.out) + row * ROW;
+#pragma unroll
+            for (int e = 0; e < ITEMS; ++e)
+                if (static_cast<uint32_t>(e) < tail) gp[e] = v[e];
+        }
     };
     auto wait1 = [&](uint64_t* bar, uint32_t ph, uint64_t b) -> bool {
         return ptx::mbar_try_wait(bar, ph) || ptx::mbar_wait_bounded(bar, ph, ptx::global_timer_ns() + b);
@@ -379,9 +343,13 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     auto heads_of = [&](int q, int k) -> uint32_t* { return ctrl->heads[SEG ? q : 0][k]; };
     // Head bits of a thread's ITEMS consecutive items (logical order).
     auto head_bits = [&](const uint32_t* hw, uint32_t thr) -> uint32_t {
-        if (!SEG) return 0u;
-        if (ITEMS == 32) return hw[thr];
-        return (hw[thr * ITEMS / 32] >> ((thr * ITEMS) & 31u)) & ((1u << ITEMS) - 1u);
+        if constexpr (!SEG) {
+            return 0u;
+        } else if constexpr (ITEMS == 32) {
+            return hw[thr];
+        } else {
+            return (hw[thr * ITEMS / 32] >> ((thr * ITEMS) & 31u)) & ((1u << ITEMS) - 1u);
+        }
     };
 
     // ======================================================== R-loader
@@ -434,12 +402,11 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                     }
                     const uint32_t t = u * G + k;
                     ctrl->r_tile[s] = t;
-                    const uint32_t bytes = bulk_bytes_of(t);
+                    const uint32_t bytes = tma_bytes_of(t);
                     ptx::mbar_arrive_expect_tx(&ctrl->rfull[s], bytes);
                     if (bytes)
-                        ptx::bulk_load_hint(rbuf + static_cast<size_t>(s) * TILE,
-                                            static_cast<const T*>(a.in) + static_cast<uint64_t>(t) * TILE, bytes,
-                                            &ctrl->rfull[s], pol);
+                        ptx::tma_load_2d(rbuf + static_cast<size_t>(s) * TILE, &tin, 0, static_cast<int32_t>(t * NROLE),
+                                         &ctrl->rfull[s], pol);
                 }
             }
             if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
@@ -486,12 +453,11 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                     }
                     const uint32_t t = u * G + k;
                     ctrl->s_tile[s] = t;
-                    const uint32_t bytes = bulk_bytes_of(t);
+                    const uint32_t bytes = tma_bytes_of(t);
                     ptx::mbar_arrive_expect_tx(&ctrl->sfull[s], bytes);
                     if (bytes)
-                        ptx::bulk_load_hint(sbuf + static_cast<size_t>(s) * TILE,
-                                            static_cast<const T*>(a.in) + static_cast<uint64_t>(t) * TILE, bytes,
-                                            &ctrl->sfull[s], pol);
+                        ptx::tma_load_2d(sbuf + static_cast<size_t>(s) * TILE, &tin, 0, static_cast<int32_t>(t * NROLE),
+                                         &ctrl->sfull[s], pol);
                 }
                 if (end) break;
             }
@@ -510,10 +476,10 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                 }
                 const uint32_t t = ctrl->s_tile[s];
                 if (t == kTileEnd) break;
-                const uint32_t bytes = bulk_bytes_of(t);
-                if (bytes)
-                    ptx::bulk_store_hint(static_cast<T*>(a.out) + static_cast<uint64_t>(t) * TILE,
-                                         sbuf + static_cast<size_t>(s) * TILE, bytes, pol);
+                // Rows past the tensor are clipped by the TMA unit.
+                if (tma_bytes_of(t))
+                    ptx::tma_store_2d(&tout, 0, static_cast<int32_t>(t * NROLE), sbuf + static_cast<size_t>(s) * TILE,
+                                      pol);
                 ptx::bulk_commit();
                 if (sn >= 1) {
                     ptx::bulk_wait_read<1>();
@@ -544,76 +510,80 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
         constexpr int kHeadBatch = 8;  // offset loads in flight per lane
         // Unsegmented scans read no head bits; the warp has nothing to do
         // (it must not fall behind the queue phases, so it leaves).
-        if (!SEG) return;
-        // For each unit of this CTA, marks the elements where a segment
-        // starts: the offsets o with tile_start <= o < tile_end, found by a
-        // search in the shared samples, then one coalesced read of the
-        // sampled block, then a forward walk over the following offsets.
-        for (uint32_t i = 0;; ++i) {
-            const int q = static_cast<int>(i % Q);
-            const uint32_t ph = (i / Q) & 1u;
-            bool ok = true;
-            if (lane == 0) ok = wait1(&ctrl->uknown[q], ph, long_budget);
-            ok = __shfl_sync(kFullMask, ok, 0);
-            __syncwarp();
-            if (!ok) {
-                if (lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
-                break;
-            }
-            const uint32_t u = ctrl->unit_of[q];
-            if (u == kTileEnd) break;
-            for (int k = 0; k < G; ++k)
-                for (int w = lane; w < kHeadWords; w += 32) heads_of(q, k)[w] = 0u;
-            __syncwarp();
-            if (SEG && nseg != 0) {
-                const uint64_t ustart = static_cast<uint64_t>(u) * G * TILE;
-                const uint64_t uend = min(ustart + static_cast<uint64_t>(G) * TILE, a.n);
-                // First sample greater than ustart (binary search in smem).
-                uint32_t lo_s = 0, hi_s = nsample;  // invariant: sample[lo_s-1] <= ustart < sample[hi_s]
-                while (lo_s < hi_s) {
-                    const uint32_t mid = (lo_s + hi_s) >> 1;
-                    if (ctrl->sample[mid] <= ustart)
-                        lo_s = mid + 1;
-                    else
-                        hi_s = mid;
+        if constexpr (!SEG) {
+            return;
+        } else {
+            // For each unit of this CTA, marks the elements where a segment
+            // starts: the offsets o with tile_start <= o < tile_end, found by a
+            // search in the shared samples, then one coalesced read of the
+            // sampled block, then a forward walk over the following offsets.
+            for (uint32_t i = 0;; ++i) {
+                const int q = static_cast<int>(i % Q);
+                const uint32_t ph = (i / Q) & 1u;
+                bool ok = true;
+                if (lane == 0) ok = wait1(&ctrl->uknown[q], ph, long_budget);
+                ok = __shfl_sync(kFullMask, ok, 0);
+                __syncwarp();
+                if (!ok) {
+                    if (lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
+                    break;
                 }
-                // The first offset >= ustart has an index in [lo_i, hi_i].
-                uint32_t lo_i = lo_s == 0 ? 0u : (lo_s - 1) * stride;
-                uint32_t hi_i = lo_s < nsample ? min(lo_s * stride, nseg) : nseg;
-                // Narrow a wide interval (many short segments) 32-fold per
-                // round: one offset per lane, the last lane below ustart wins.
-                while (hi_i - lo_i > kHeadBatch * 32u) {
-                    const uint32_t step = (hi_i - lo_i + 31u) / 32u;
-                    const uint32_t idx = min(lo_i + lane * step, nseg - 1u);
-                    const uint32_t below = __ballot_sync(kFullMask, sg.offsets[idx] < ustart);
-                    if (below == 0u) break;  // offsets[lo_i] >= ustart already
-                    const uint32_t last = 31u - static_cast<uint32_t>(__clz(below));
-                    hi_i = min(lo_i + (last + 1u) * step, hi_i);
-                    lo_i = lo_i + last * step;
-                }
-                // Walk forward from lo_i, kHeadBatch loads of 32 offsets in
-                // flight per round, until an offset at or past uend.
-                for (uint32_t cur = lo_i; cur < nseg; cur += kHeadBatch * 32u) {
-                    uint32_t o[kHeadBatch];
-#pragma unroll
-                    for (int j = 0; j < kHeadBatch; ++j) {
-                        const uint32_t idx = cur + static_cast<uint32_t>(j) * 32u + lane;
-                        o[j] = idx < nseg ? sg.offsets[idx] : 0xFFFFFFFFu;
+                const uint32_t u = ctrl->unit_of[q];
+                if (u == kTileEnd) break;
+                for (int k = 0; k < G; ++k)
+                    for (int w = lane; w < kHeadWords; w += 32) heads_of(q, k)[w] = 0u;
+                __syncwarp();
+                if (SEG && nseg != 0) {
+                    const uint64_t ustart = static_cast<uint64_t>(u) * G * TILE;
+                    const uint64_t uend = min(ustart + static_cast<uint64_t>(G) * TILE, a.n);
+                    // First sample greater than ustart (binary search in smem).
+                    uint32_t lo_s = 0, hi_s = nsample;  // invariant: sample[lo_s-1] <= ustart < sample[hi_s]
+                    while (lo_s < hi_s) {
+                        const uint32_t mid = (lo_s + hi_s) >> 1;
+                        if (ctrl->sample[mid] <= ustart)
+                            lo_s = mid + 1;
+                        else
+                            hi_s = mid;
                     }
-                    bool past = false;
-#pragma unroll
-                    for (int j = 0; j < kHeadBatch; ++j) {
-                        if (o[j] >= ustart && o[j] < uend) {
-                            const uint32_t pos = static_cast<uint32_t>(o[j] - ustart);
-                            atomicOr(&heads_of(q, static_cast<int>(pos / TILE))[(pos % TILE) >> 5], 1u << (pos & 31u));
+                    // The first offset >= ustart has an index in [lo_i, hi_i].
+                    uint32_t lo_i = lo_s == 0 ? 0u : (lo_s - 1) * stride;
+                    uint32_t hi_i = lo_s < nsample ? min(lo_s * stride, nseg) : nseg;
+                    // Narrow a wide interval (many short segments) 32-fold per
+                    // round: one offset per lane, the last lane below ustart wins.
+                    while (hi_i - lo_i > kHeadBatch * 32u) {
+                        const uint32_t step = (hi_i - lo_i + 31u) / 32u;
+                        const uint32_t idx = min(lo_i + lane * step, nseg - 1u);
+                        const uint32_t below = __ballot_sync(kFullMask, sg.offsets[idx] < ustart);
+                        if (below == 0u) break;  // offsets[lo_i] >= ustart already
+                        const uint32_t last = 31u - static_cast<uint32_t>(__clz(below));
+                        hi_i = min(lo_i + (last + 1u) * step, hi_i);
+                        lo_i = lo_i + last * step;
+                    }
+                    // Walk forward from lo_i, kHeadBatch loads of 32 offsets in
+                    // flight per round, until an offset at or past uend.
+                    for (uint32_t cur = lo_i; cur < nseg; cur += kHeadBatch * 32u) {
+                        uint32_t o[kHeadBatch];
+    #pragma unroll
+                        for (int j = 0; j < kHeadBatch; ++j) {
+                            const uint32_t idx = cur + static_cast<uint32_t>(j) * 32u + lane;
+                            o[j] = idx < nseg ? sg.offsets[idx] : 0xFFFFFFFFu;
                         }
-                        past = past || o[j] >= uend;
+                        bool past = false;
+    #pragma unroll
+                        for (int j = 0; j < kHeadBatch; ++j) {
+                            if (o[j] >= ustart && o[j] < uend) {
+                                const uint32_t pos = static_cast<uint32_t>(o[j] - ustart);
+                                atomicOr(&heads_of(q, static_cast<int>(pos / TILE))[(pos % TILE) >> 5], 1u << (pos & 31u));
+                            }
+                            past = past || o[j] >= uend;
+                        }
+                        if (__any_sync(kFullMask, past)) break;
                     }
-                    if (__any_sync(kFullMask, past)) break;
                 }
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&ctrl->uheads[q]);
             }
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&ctrl->uheads[q]);
+    
         }
     }
     // ======================================================== lookback
@@ -672,8 +642,8 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     else if (warp < kWarpFinal) {
         const uint32_t r = tid - kWarpReduce * 32;
         const uint32_t rw = warp - kWarpReduce;
-        const uint32_t rot = r & 7u;
         ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
+        // State of the unit so far (the same in every reduce thread).
         S unit_agg = Op::zero();
         bool unit_flag = false;
         for (uint32_t rn = 0;; ++rn) {
@@ -688,48 +658,32 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
             if (SEG && live && k == 0)
                 ok = ptx::mbar_try_wait(&ctrl->uheads[q], (i / Q) & 1u) ||
                      ptx::mbar_wait_bounded(&ctrl->uheads[q], (i / Q) & 1u, ptx::global_timer_ns() + long_budget);
-            const T* sb = rbuf + static_cast<size_t>(s) * TILE;
-            const uint32_t cnt = live ? count_of(t) : 0u;
             T v[ITEMS];
-            if (cnt == static_cast<uint32_t>(TILE)) {
-#pragma unroll
-                for (int c8 = 0; c8 < CHUNKS; ++c8) {
-                    const uint32_t c = (c8 + rot) & (CHUNKS - 1);
-                    const Chunk<T> qv = *reinterpret_cast<const Chunk<T>*>(sb + r * ITEMS + c * EPC);
-#pragma unroll
-                    for (int e = 0; e < EPC; ++e) v[c8 * EPC + e] = qv.v[e];
-                }
-            } else {
-                const uint32_t bulk_elems = live ? bulk_bytes_of(t) / static_cast<uint32_t>(sizeof(T)) : 0u;
-                const uint64_t gbase = static_cast<uint64_t>(live ? t : 0u) * TILE;
-#pragma unroll
-                for (int e = 0; e < ITEMS; ++e) {
-                    const uint32_t li = r * ITEMS + e;
-                    T x = T(0);
-                    if (li < bulk_elems)
-                        x = sb[li];
-                    else if (li < cnt)
-                        x = static_cast<const T*>(a.in)[gbase + li];
-                    v[e] = x;
-                }
-            }
+            load_row(rbuf + static_cast<size_t>(s) * TILE, live ? t : a.num_tiles, r, v);
             const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), r) : 0u;
-            const uint32_t rrot = cnt == static_cast<uint32_t>(TILE) ? rot : 0u;
-            // Warp aggregate (items beyond cnt are zero and carry no head),
-            // formed exactly as the finalize warps form it for floating point:
-            // chunk aggregates in logical order, then a lane-order scan. Warps
-            // whose items hold no segment head take the plain path.
-            S ca[CHUNKS];
-            S tv;
-            bool tf;
-            if (SEG && __any_sync(kFullMask, hb != 0u))
-                thread_and_warp_scan<Op, CHUNKS, EPC, SEG, REORDER, false>(v, hb, rrot, lane, ca, tv, tf);
-            else
-                thread_and_warp_scan<Op, CHUNKS, EPC, false, !std::is_integral<T>::value,
-                                     std::is_integral<T>::value>(v, 0u, rrot, lane, ca, tv, tf);
+            // Thread aggregate, then the warp's inclusive scan of them; warps
+            // whose items hold no segment head take the flag-free path.
+            const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
+            S wv;
+            bool wf;
+            if (heads_here) {
+                wv = thread_aggregate<Op, ITEMS, true>(v, hb);
+                wf = hb != 0u;
+                warp_scan_incl<Op, true>(wv, wf, lane);
+            } else {
+                wv = thread_aggregate<Op, ITEMS, false>(v, 0u);
+                wf = false;
+                warp_scan_incl<Op, false>(wv, wf, lane);
+            }
+            S xv = Op::shfl_up(wv, 1);
+            bool xf = SEG ? __shfl_up_sync(kFullMask, wf, 1) : false;
+            if (lane == 0) {
+                xv = Op::zero();
+                xf = false;
+            }
             if (lane == 31) {
-                ctrl->r_wtot[rn & 1u][rw] = tv;
-                ctrl->r_wflag[rn & 1u][rw] = tf;
+                ctrl->r_wtot[rn & 1u][rw] = wv;
+                ctrl->r_wflag[rn & 1u][rw] = wf;
             }
             const bool stop = named_bar_or(1, NROLE, !live || !ok);
             if (lane == 0 && live) ptx::mbar_arrive(&ctrl->rfree[s]);
@@ -740,14 +694,29 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                 }
                 break;
             }
-            if (r == 0) {
-                S agg = Op::zero();
-                bool af = false;
+            // The state before this thread within the unit, for the scan
+            // pass; then the unit state moves past the tile.
+            S pre = unit_agg;
+            bool pf = unit_flag;
+            S tile_agg = Op::zero();
+            bool tile_f = false;
 #pragma unroll
-                for (int w2 = 0; w2 < RW; ++w2)
-                    seg_combine<Op>(agg, af, ctrl->r_wtot[rn & 1u][w2], ctrl->r_wflag[rn & 1u][w2] != 0);
-                seg_combine<Op>(unit_agg, unit_flag, agg, af);
-                if (k == G - 1) {
+            for (int w2 = 0; w2 < RW; ++w2) {
+                const S x = ctrl->r_wtot[rn & 1u][w2];
+                const bool xfl = ctrl->r_wflag[rn & 1u][w2] != 0;
+                if (static_cast<uint32_t>(w2) < rw) seg_combine<Op>(pre, pf, x, xfl);
+                seg_combine<Op>(tile_agg, tile_f, x, xfl);
+            }
+            seg_combine<Op>(pre, pf, xv, xf);
+            ctrl->tpre[q][k][r] = Op::norm(pre);
+            if (SEG) {
+                const uint32_t fb = __ballot_sync(kFullMask, pf);
+                if (lane == 0) ctrl->tflag[q][k][rw] = fb;
+            }
+            seg_combine<Op>(unit_agg, unit_flag, tile_agg, tile_f);
+            unit_agg = Op::norm(unit_agg);
+            if (k == G - 1) {
+                if (r == 0) {
                     const uint32_t u = t / G;
                     const C chain = Op::to_chain(unit_agg);
                     ptx::st_relaxed_b128(desc + u, seg_pack(u == 0 ? kInclusive : kAggregate, unit_flag, epoch,
@@ -755,9 +724,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
                     ctrl->uagg[q] = chain;
                     ctrl->uflag[q] = unit_flag;
                     ptx::mbar_arrive(&ctrl->ureduced[q]);
-                    unit_agg = Op::zero();
-                    unit_flag = false;
                 }
+                unit_agg = Op::zero();
+                unit_flag = false;
             }
         }
     }
@@ -765,138 +734,42 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1) scan_seg_kernel
     else {
         const uint32_t f = tid - kWarpFinal * 32;
         const uint32_t fw = warp - kWarpFinal;
-        const uint32_t rot = f & 7u;
-        S run = Op::zero();  // state before the current tile
-        bool go = true;
-        for (uint32_t sn = 0; go; ++sn) {
+        S run = Op::zero();  // the unit's prefix from the lookback
+        for (uint32_t sn = 0;; ++sn) {
             const int s = static_cast<int>(sn % SS);
             const uint32_t i = sn / G;
             const int k = static_cast<int>(sn % G);
             const int q = static_cast<int>(i % Q);
-            const bool ok = ptx::mbar_try_wait(&ctrl->sfull[s], (sn / SS) & 1u) ||
-                            ptx::mbar_wait_bounded(&ctrl->sfull[s], (sn / SS) & 1u, ptx::global_timer_ns() + long_budget);
+            const bool ok = __all_sync(kFullMask, ptx::mbar_try_wait(&ctrl->sfull[s], (sn / SS) & 1u) ||
+                                                      ptx::mbar_wait_bounded(&ctrl->sfull[s], (sn / SS) & 1u,
+                                                                             ptx::global_timer_ns() + long_budget));
             const uint32_t t = ok ? ctrl->s_tile[s] : kTileEnd;
-            const bool live = t != kTileEnd;
-            T* sb = sbuf + static_cast<size_t>(s) * TILE;
-            const uint32_t cnt = live ? count_of(t) : 0u;
-            const bool full_tile = cnt == static_cast<uint32_t>(TILE);
-            const uint32_t bulk_elems = live ? bulk_bytes_of(t) / static_cast<uint32_t>(sizeof(T)) : 0u;
-            const uint64_t gbase = static_cast<uint64_t>(live ? t : 0u) * TILE;
-            T v[ITEMS];
-            if (full_tile) {
-#pragma unroll
-                for (int c8 = 0; c8 < CHUNKS; ++c8) {
-                    const uint32_t c = (c8 + rot) & (CHUNKS - 1);
-                    const Chunk<T> qv = *reinterpret_cast<const Chunk<T>*>(sb + f * ITEMS + c * EPC);
-#pragma unroll
-                    for (int e = 0; e < EPC; ++e) v[c8 * EPC + e] = qv.v[e];
-                }
-            } else {
-#pragma unroll
-                for (int e = 0; e < ITEMS; ++e) {
-                    const uint32_t li = f * ITEMS + e;
-                    T x = T(0);
-                    if (li < bulk_elems)
-                        x = sb[li];
-                    else if (li < cnt)
-                        x = static_cast<const T*>(a.in)[gbase + li];
-                    v[e] = x;
-                }
-            }
-            // The head warp may still be marking this unit: wait for it (its
-            // bits stay valid until this unit's queue entry is released).
-            bool hok = true;
-            if (SEG && live && k == 0)
-                hok = ptx::mbar_try_wait(&ctrl->uheads[q], (i / Q) & 1u) ||
-                      ptx::mbar_wait_bounded(&ctrl->uheads[q], (i / Q) & 1u, ptx::global_timer_ns() + long_budget);
-            if (!hok) raise_error(a.hdr, kErrPipelineTimeout);
-            const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), f) : 0u;
-            const uint32_t rrot = full_tile ? rot : 0u;
-            // Chunk aggregates (logical order) and the warp's inclusive scan
-            // of the thread aggregates; then exclusive by one lane.
-            S ca[CHUNKS];
-            S wv;
-            bool wf;
-            const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
-            const uint32_t cmask =
-                heads_here ? thread_and_warp_scan<Op, CHUNKS, EPC, SEG, true, false>(v, hb, rrot, lane, ca, wv, wf)
-                           : thread_and_warp_scan<Op, CHUNKS, EPC, false, true, false>(v, 0u, rrot, lane, ca, wv, wf);
-            S xv = Op::shfl_up(wv, 1);
-            bool xf = SEG ? __shfl_up_sync(kFullMask, wf, 1) : false;
-            if (lane == 0) {
-                xv = Op::zero();
-                xf = false;
-            }
-            if (lane == 31) {
-                ctrl->f_wtot[sn & 1u][fw] = wv;
-                ctrl->f_wflag[sn & 1u][fw] = wf;
-            }
-            if (named_bar_or(2, NROLE, !live)) {
-                if (!ok && f == 0) raise_error(a.hdr, kErrPipelineTimeout);
-                if (lane == 0) ptx::mbar_arrive(&ctrl->sdone[s]);
-                go = false;
+            if (t == kTileEnd) {
+                if (!ok && lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
+                if (lane == 0) ptx::mbar_arrive(&ctrl->sdone[s]);  // lets the storer see the end
                 break;
             }
+            T* sb = sbuf + static_cast<size_t>(s) * TILE;
+            T v[ITEMS];
+            load_row(sb, t, f, v);
             if (k == 0) {
+                // The unit's prefix; it also orders this warp after the head
+                // warp's bits and the reduce pass's per-thread prefixes.
                 bool pok = ptx::mbar_try_wait(&ctrl->uprefix[q], (i / Q) & 1u) ||
                            ptx::mbar_wait_bounded(&ctrl->uprefix[q], (i / Q) & 1u, ptx::global_timer_ns() + long_budget);
                 pok = __all_sync(kFullMask, pok);
                 if (!pok && lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
                 run = Op::from_chain(ctrl->upre[q]);
             }
-            // State before this thread: tile prefix, earlier warps, earlier lanes.
-            S base = run;
-            bool bf = false;
-            S tile_agg = Op::zero();
-            bool tile_f = false;
-#pragma unroll
-            for (int w2 = 0; w2 < RW; ++w2) {
-                const S x = ctrl->f_wtot[sn & 1u][w2];
-                const bool xfl = ctrl->f_wflag[sn & 1u][w2] != 0;
-                if (static_cast<uint32_t>(w2) < fw) seg_combine<Op>(base, bf, x, xfl);
-                seg_combine<Op>(tile_agg, tile_f, x, xfl);
-            }
-            seg_combine<Op>(base, bf, xv, xf);
-            {
-                bool rf = false;
-                seg_combine<Op>(run, rf, tile_agg, tile_f);
-            }
-            // State before each chunk (logical order), then back to register
-            // order; then CHUNKS independent chains of EPC items.
-            {
-                S st = base;
-                bool sf = false;
-#pragma unroll
-                for (int c = 0; c < CHUNKS; ++c) {
-                    const S x = ca[c];
-                    ca[c] = st;
-                    seg_combine<Op>(st, sf, x, (cmask >> c) & 1u);
-                }
-            }
-            rotate_chunks<S, CHUNKS, 1>(ca, (CHUNKS - rrot) & (CHUNKS - 1));
-            if (heads_here)
-                chunk_outputs<Op, CHUNKS, EPC, SEG, INCL>(v, ca, hb, rrot);
+            const uint32_t hb = SEG ? head_bits(heads_of(q, k), f) : 0u;
+            const S pre = ctrl->tpre[q][k][f];
+            const bool pf = SEG && ((ctrl->tflag[q][k][fw] >> lane) & 1u);
+            const S base = pf ? pre : Op::combine(run, pre);
+            if (SEG && __any_sync(kFullMask, hb != 0u))
+                thread_outputs<Op, ITEMS, true, INCL>(v, base, hb);
             else
-                chunk_outputs<Op, CHUNKS, EPC, false, INCL>(v, ca, 0u, rrot);
-            if (full_tile) {
-#pragma unroll
-                for (int c8 = 0; c8 < CHUNKS; ++c8) {
-                    const uint32_t c = (c8 + rot) & (CHUNKS - 1);
-                    Chunk<T> qv;
-#pragma unroll
-                    for (int e = 0; e < EPC; ++e) qv.v[e] = v[c8 * EPC + e];
-                    *reinterpret_cast<Chunk<T>*>(sb + f * ITEMS + c * EPC) = qv;
-                }
-            } else {
-#pragma unroll
-                for (int e = 0; e < ITEMS; ++e) {
-                    const uint32_t li = f * ITEMS + e;
-                    if (li < bulk_elems)
-                        sb[li] = v[e];
-                    else if (li < cnt)
-                        static_cast<T*>(a.out)[gbase + li] = v[e];
-                }
-            }
+                thread_outputs<Op, ITEMS, false, INCL>(v, base, 0u);
+            store_row(sb, t, f, v);
             ptx::fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {

@@ -7,30 +7,44 @@
 
 namespace gps {
 
-// 4 reduce + 4 finalize warps over 16 KB tiles, 4 reduce-pass and 9
-// scan-pass stages, 6 units in flight per CTA (measured on GB300: 4 + 9
-// beats 5 + 8 by 3-8% on the batched workloads). The unit (1 or 4 tiles) and
-// the CTA count come from the plan's launch configuration (GenericConfig).
+// 4 reduce + 4 finalize warps over 16 KB tiles, 6 units in flight per CTA.
+// Stages: as many as fit in 227 KB of shared memory next to the control
+// block (whose per-thread prefixes and head bitmaps grow with the state size
+// and the unit), taken as 4 reduce-pass + 9 scan-pass stages when 13 fit
+// (measured on GB300: 4 + 9 beats 5 + 8 by 3-8% on the batched workloads),
+// else 4 + 8, else 3 + 8. The unit (1 or 4 tiles) and the CTA count come from
+// the plan's launch configuration (GenericConfig).
 constexpr int kSegWarps = 4;
-constexpr int kSegRStages = 4;
-constexpr int kSegSStages = 9;
 constexpr int kSegQueue = 6;
+constexpr size_t kMaxSmem = 232448;
+
+template <class Op, int G, bool SEG>
+struct SegStages {
+    static constexpr bool k13 = seg_smem_bytes<Op, kSegWarps, 4, 9, kSegQueue, G, SEG>() <= kMaxSmem;
+    static constexpr bool k12 = seg_smem_bytes<Op, kSegWarps, 4, 8, kSegQueue, G, SEG>() <= kMaxSmem;
+    static constexpr int RS = (k13 || k12) ? 4 : 3;
+    static constexpr int SS = k13 ? 9 : 8;
+    static_assert(seg_smem_bytes<Op, kSegWarps, RS, SS, kSegQueue, G, SEG>() <= kMaxSmem, "227 KB per CTA");
+};
 
 template <class Op, bool INCL, bool SEG, int UNIT>
 cudaError_t launch_seg_t(const ScanArgs& a, const SegArgs& sg, const GenericConfig& cfg, int num_sms,
                          cudaStream_t stream, LaunchInfo* info) {
-    auto kern = scan_seg_kernel<Op, kSegWarps, kSegRStages, kSegSStages, kSegQueue, UNIT, INCL, SEG>;
-    constexpr size_t smem = seg_smem_bytes<Op, kSegWarps, kSegRStages, kSegSStages, kSegQueue, UNIT, SEG>();
-    static_assert(smem <= 232448, "227 KB of shared memory per CTA");
+    using St = SegStages<Op, UNIT, SEG>;
+    auto kern = scan_seg_kernel<Op, kSegWarps, St::RS, St::SS, kSegQueue, UNIT, INCL, SEG>;
+    constexpr size_t smem = seg_smem_bytes<Op, kSegWarps, St::RS, St::SS, kSegQueue, UNIT, SEG>();
     constexpr int threads = SegShape<Op, kSegWarps>::kThreads;
+    RowMaps maps;
+    cudaError_t err = encode_row_maps(a.in, a.out, a.n, static_cast<uint32_t>(sizeof(typename Op::T)), &maps);
+    if (err != cudaSuccess) return err;
     int occ = 0;
-    cudaError_t err = resident_ctas_per_sm(kern, threads, smem, &occ);
+    err = resident_ctas_per_sm(kern, threads, smem, &occ);
     if (err != cudaSuccess) return err;
     const uint32_t units = (a.num_tiles + UNIT - 1) / UNIT;
     const int ctas = std::max(1, occ * num_sms / static_cast<int>(std::max(1u, cfg.ctas_div)));
     const int grid = persistent_grid(units, 1, ctas);
     if (info) *info = LaunchInfo{grid, threads, smem};
-    kern<<<grid, threads, smem, stream>>>(a, sg);
+    kern<<<grid, threads, smem, stream>>>(a, sg, maps.in, maps.out);
     return cudaGetLastError();
 }
 
