@@ -33,11 +33,15 @@ template <>
 __device__ __forceinline__ float shfl_up_any(float s, uint32_t d) { return __shfl_up_sync(0xFFFFFFFFu, s, d); }
 
 // ------------------------------------------------------------- integers
+// kL2Prefetch: the kernel prefetches each unit into L2 when it takes the
+// unit (pays off for the streaming-bound operations, measured 3-4% on GB300;
+// the compensated scan is bound by its arithmetic and loses 4% instead).
 template <typename U>
 struct OpInt {
     using T = U;
     using S = U;
     using C = U;
+    static constexpr bool kL2Prefetch = true;
     __device__ static S zero() { return 0; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
@@ -65,6 +69,7 @@ struct OpF32 {
     using T = float;
     using S = float;
     using C = float;
+    static constexpr bool kL2Prefetch = true;
     __device__ static S zero() { return 0.0f; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
@@ -104,6 +109,7 @@ struct OpF32C {
     using T = float;
     using S = F2;
     using C = double;
+    static constexpr bool kL2Prefetch = false;
     __device__ static S zero() { return F2{0.0f, 0.0f}; }
     __device__ static S lift(T x) { return F2{x, 0.0f}; }
     __device__ static S add(S a, S b) {

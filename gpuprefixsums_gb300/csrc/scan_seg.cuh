@@ -370,13 +370,22 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             for (uint32_t i = 0; ok; ++i) {
                 const int q = static_cast<int>(i % Q);
                 if (i >= Q && !wait1(&ctrl->ufree[q], ((i - Q) / Q) & 1u, long_budget)) break;
-                // The unit id is taken only now, when its loads follow (see
-                // scan_l2.cuh). No L2 prefetch here: this kernel is bound by
-                // its per-tile work, and the prefetched lines only crowd the
-                // L2 (measured: 7% slower on the 4096-segment batch).
+                // The unit id is taken only now, when its loads follow, and
+                // the unit's full rows are prefetched into L2 (see
+                // scan_l2.cuh; per operation, Op::kL2Prefetch).
                 const uint32_t u = resolve(acquire());
                 ctrl->unit_of[q] = u;
                 ptx::mbar_arrive(&ctrl->uknown[q]);
+                if (Op::kL2Prefetch && u != kTileEnd) {
+#pragma unroll
+                    for (int k = 0; k < G; ++k) {
+                        if (tma_bytes_of(u * G + k) == 0) continue;
+                        const uint64_t r0 = static_cast<uint64_t>(u * G + k) * NROLE;
+                        const uint64_t r1 = r0 + NROLE < rows_full ? r0 + NROLE : rows_full;
+                        ptx::bulk_prefetch_l2(static_cast<const T*>(a.in) + r0 * ROW, static_cast<uint32_t>((r1 - r0) * 128),
+                                              pol);
+                    }
+                }
                 if (u == kTileEnd) {
                     for (uint32_t m = 1; m < LW && ok; ++m) {
                         const uint32_t i2 = i + m;
