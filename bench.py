@@ -151,6 +151,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(window)}
 
 
+def max_over_ranks(value, dist=None, device="cuda"):
+    """The slowest rank's figure (times are maxed over ranks); the value
+    itself on a single process."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_loop(fn, steps, stream):
     import torch
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -472,10 +483,7 @@ def run_ours(args, world, rank, local):
         dist.barrier()
     clocks = sampler.stop(t0, t1)
     plan.check(stream)
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     alg_bytes = n * 8
     value = world * alg_bytes / (ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
@@ -530,10 +538,7 @@ def run_ours(args, world, rank, local):
         for _ in range(args.e2e_steps):
             plan.scan_host(h_in.data_ptr(), h_out.data_ptr(), n, stream=stream)
         e2e_s = (time.perf_counter() - te) / args.e2e_steps
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist)
         e2e = {"value": round(world * alg_bytes / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": n * 4,
                "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_s * 1e3, 3),
                "path": "gps_scan_host: pinned host -> device -> host, chunked and overlapped"}
