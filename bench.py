@@ -27,7 +27,9 @@ Reported (one JSON line on rank 0):
                compensated FP32 throughput and errors against a float64 scan;
   mixed        10,000 scans, lengths Zipf(1.2) in [32, 2^22], dtype per scan
                from {u32, u64, compensated f32}, plus a 2^28-element u32
-               Bernoulli(0.3) flag scan, all in one CUDA graph.
+               Bernoulli(0.3) flag scan, all in one CUDA graph;
+  select       stream compaction of 2^28 u32 values by Bernoulli(0.3) flag
+               bytes in one launch, beside CUB's DeviceSelect::Flagged.
 With --impl reference the line times the reference's own algorithm on the
 host instead (the oracle's multi-threaded restatement, all host threads): the
 reference ships no CPU scan of its own.
@@ -298,6 +300,55 @@ def run_batched(stream, copy_gbs, reps=20):
             "identical_to_looped": same, "autotuned": tuned, "launches_per_step": 1}
 
 
+def run_select(stream, copy_gbs, reps=20):
+    """Stream compaction of 2^28 u32 values by Bernoulli(0.3) flag bytes:
+    the fused select against CUB's DeviceSelect::Flagged on the same data."""
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    from gpuprefixsums_gb300 import build as gbuild
+    n = 1 << 28
+    gen = torch.Generator(device="cuda").manual_seed(303)
+    x = torch.randint(-2 ** 31, 2 ** 31 - 1, (n,), dtype=torch.int32, device="cuda", generator=gen)
+    fl = (torch.rand(n, device="cuda", generator=gen) < 0.3).to(torch.uint8)
+    out = torch.empty_like(x)
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    res = {"workload": "select 2^28 u32 by Bernoulli(0.3) flag bytes (fused flag scan + scatter, 1 launch)"}
+    with Plan("csdl", "u32", max_n=n) as plan:
+        step = lambda: plan.select(x, fl, out=out, num_selected=cnt, stream=stream)  # noqa: E731
+        for _ in range(3):
+            step()
+        ms = time_loop(step, reps, stream)
+        plan.check(stream)
+    c = int(cnt.item())
+    if not torch.equal(out[:c], torch.masked_select(x, fl.bool())):
+        raise SystemExit("bench: select result is wrong; refusing to report a number")
+    alg = n * 5 + c * 4
+    res.update({"selected": c, "ms": round(ms, 4), "gbs": round(alg / (ms * 1e-3) / 1e9, 2),
+                "elements_per_s": round(n / (ms * 1e-3), 1),
+                "pct_of_copy": round(100.0 * alg / (ms * 1e-3) / 1e9 / copy_gbs, 2) if copy_gbs else None,
+                "bytes_per_element": round(alg / n, 3)})
+    try:
+        cub = ctypes.CDLL(gbuild.build_cub_compare())
+        cub.gps_cub_select_u32.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_uint64, ctypes.c_void_p,
+                                                                     ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]
+        tb = ctypes.c_size_t(0)
+        cub.gps_cub_select_u32(x.data_ptr(), fl.data_ptr(), out.data_ptr(), cnt.data_ptr(), n, None, ctypes.byref(tb),
+                               None)
+        temp = torch.empty(max(1, tb.value), dtype=torch.uint8, device="cuda")
+        sp = ctypes.c_void_p(stream.cuda_stream)
+        cub_call = lambda: cub.gps_cub_select_u32(x.data_ptr(), fl.data_ptr(), out.data_ptr(),  # noqa: E731
+                                                  cnt.data_ptr(), n, temp.data_ptr(), ctypes.byref(tb), sp)
+        for _ in range(3):
+            cub_call()
+        cub_ms = time_loop(cub_call, reps, stream)
+        res["cub_select_ms"] = round(cub_ms, 4)
+        res["ours_vs_cub"] = round(cub_ms / ms, 3)
+    except Exception as e:  # comparison only
+        res["cub_error"] = str(e)[:200]
+    return res
+
+
 def fp_errors_vs_f64(got, ref):
     """max / median relative prefix error (nonzero reference prefixes) and
     relative error of the final sum, against a float64 scan."""
@@ -547,6 +598,7 @@ def run_ours(args, world, rank, local):
             extras["batched"] = run_batched(stream, compare.get("d2d_copy_gbs"))
             extras["fp32"] = run_fp32(stream)
             extras["mixed"] = run_mixed(stream, compare.get("d2d_copy_gbs"))
+            extras["select"] = run_select(stream, compare.get("d2d_copy_gbs"))
 
         if rank == 0 and world == 1:
             import oracle

@@ -434,6 +434,48 @@ gps_status gps_plan_generic_config(gps_plan p, int segmented, uint64_t n, uint32
     return GPS_OK;
 }
 
+gps_status gps_select_flagged(gps_plan p, const void* d_in, const uint8_t* d_flags, void* d_out, uint64_t n,
+                              uint64_t* d_num_selected, gps_stream_t stream) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (p->algo != GPS_ALGO_CSDL) return fail(GPS_ERR_UNSUPPORTED, "select runs on chained-scan plans (GPS_ALGO_CSDL)");
+    if (d_num_selected == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL count pointer");
+    if ((reinterpret_cast<uintptr_t>(d_num_selected) & 7u) != 0)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "the count must be 8-byte aligned");
+    gps_status st = check_device(p);
+    if (st != GPS_OK) return st;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        const cudaError_t err = cudaMemsetAsync(d_num_selected, 0, sizeof(uint64_t), s);
+        return err == cudaSuccess ? GPS_OK : cuda_fail(err, "clearing the count");
+    }
+    if (n > p->max_n)
+        return fail(GPS_ERR_SIZE_EXCEEDS_PLAN, "requested size %llu exceeds the plan's maximum %llu",
+                    static_cast<unsigned long long>(n), static_cast<unsigned long long>(p->max_n));
+    if (d_in == nullptr || d_flags == nullptr || d_out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL pointer");
+    const size_t es = gps::dtype_size(p->dtype);
+    const uintptr_t i = reinterpret_cast<uintptr_t>(d_in), fl = reinterpret_cast<uintptr_t>(d_flags);
+    const uintptr_t o = reinterpret_cast<uintptr_t>(d_out);
+    if (((i | fl) & 15u) != 0) return fail(GPS_ERR_INVALID_ARGUMENT, "values and flags must be 16-byte aligned");
+    if ((o & (es - 1)) != 0) return fail(GPS_ERR_INVALID_ARGUMENT, "output must be aligned to the element size");
+    const uint64_t bytes = n * es;
+    if ((o < i + bytes && i < o + bytes) || (o < fl + n && fl < o + bytes))
+        return fail(GPS_ERR_INVALID_ARGUMENT, "the output overlaps the values or the flags");
+    if ((reinterpret_cast<uintptr_t>(p->desc16) & 15u) != 0)
+        return fail(GPS_ERR_CUDA, "internal: misaligned descriptor region");
+    gps::ScanArgs a{};
+    a.in = d_in;
+    a.out = d_out;
+    a.n = n;
+    a.num_tiles = static_cast<uint32_t>((n + gps::select_tile_elems(es) - 1) / gps::select_tile_elems(es));
+    a.hdr = p->hdr16;
+    a.desc = p->desc16;
+    a.carry_out = d_num_selected;
+    a.wait_budget_ns = p->wait_budget_ns;
+    const cudaError_t err = gps::launch_select(es, a, d_flags, p->num_sms, s, &p->last_launch);
+    if (err != cudaSuccess) return cuda_fail(err, "select launch");
+    return GPS_OK;
+}
+
 gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void* h_out, uint64_t n,
                          gps_stream_t stream) {
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");

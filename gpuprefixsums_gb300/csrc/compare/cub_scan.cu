@@ -3,6 +3,7 @@
 // (GPUPrefixSumsCUDA/CubDispatcher.cuh:32-76). Built as libgps_cub.so, apart
 // from the scan library; nothing in libgps.so calls CUB.
 #include <cub/device/device_scan.cuh>
+#include <cub/device/device_select.cuh>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -32,5 +33,14 @@ int gps_cub_scan_u64(int inclusive, const void* in, void* out, uint64_t n, void*
     else
         err = cub::DeviceScan::ExclusiveSum(temp, *temp_bytes, i, o, static_cast<int64_t>(n), stream);
     return static_cast<int>(err);
+}
+
+// Query (temp == nullptr) or run CUB's DeviceSelect::Flagged of n u32 with
+// one flag byte each; the count goes to *num_selected (device, int64).
+int gps_cub_select_u32(const void* in, const void* flags, void* out, void* num_selected, uint64_t n, void* temp,
+                       size_t* temp_bytes, cudaStream_t stream) {
+    return static_cast<int>(cub::DeviceSelect::Flagged(
+        temp, *temp_bytes, static_cast<const uint32_t*>(in), static_cast<const uint8_t*>(flags),
+        static_cast<uint32_t*>(out), static_cast<int64_t*>(num_selected), static_cast<int64_t>(n), stream));
 }
 }

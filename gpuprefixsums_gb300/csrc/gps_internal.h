@@ -149,6 +149,12 @@ cudaError_t launch_seg_f32(bool inclusive, const ScanArgs& a, const SegArgs* sg,
 cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
                             int num_sms, cudaStream_t stream, LaunchInfo* info);
 
+// Stream compaction by flag bytes (select.cu): elements per tile for an
+// element size, and the launch. a.carry_out receives the count (uint64).
+uint32_t select_tile_elems(size_t elem_size);
+cudaError_t launch_select(size_t elem_size, const ScanArgs& a, const uint8_t* flags, int num_sms, cudaStream_t stream,
+                          LaunchInfo* info);
+
 uint32_t csdl_tile_elems(gps_dtype dtype);
 // Sets the text gps_last_error() returns on this host thread.
 void record_error(const char* msg);

@@ -1,0 +1,518 @@
+// Stream compaction (select by flags): the flag scan fused with the scatter,
+// in one single-pass launch.
+//
+// out[0 .. count) receives, in order, the elements in[i] whose flag byte is
+// non-zero; count goes to *num_selected. The structure is the chained scan's
+// (decoupled lookback over 64-bit counts, as ChainedScanDecoupledLookback.cuh:
+// 79-139 does for sums), with the two passes of scan_l2.cuh:
+//   reduce pass  bulk-load a tile's flags (1 byte per element) with an L2
+//                evict-last policy, count the selected elements of each
+//                thread, leave every thread its count-prefix within the unit
+//                and publish the unit's count;
+//   scan pass    once the previous unit's prefix is known, bulk-load the
+//                tile's values (HBM) and flags (again, from L2), compact each
+//                thread's selected values into a shared-memory staging tile at
+//                their tile-local positions, and copy the staged run out with
+//                coalesced stores at the unit prefix.
+// HBM sees the flags and values once each and only the selected values
+// written: (sizeof(V) + 1) bytes read and p * sizeof(V) written per element
+// for a selected fraction p.
+//
+// Warps: 0 R-loader (flags), 1 S-loader (values + flags), 2..4 lookback,
+// then 4 reduce and 4 finalize warps. Every wait is bounded by the plan's
+// budget.
+#include "launch_util.h"
+#include "scan_pipeline.cuh"
+
+namespace gps {
+namespace {
+
+constexpr int kSelWarps = 4;                 // reduce warps = finalize warps
+constexpr int kSelRole = kSelWarps * 32;     // threads per role
+constexpr int kSelLookback = 3;
+constexpr int kSelThreads = 32 * (2 + kSelLookback + 2 * kSelWarps);
+constexpr int kSelRS = 8;   // flag stages of the reduce pass
+constexpr int kSelSS = 8;   // value + flag stages of the scan pass
+constexpr int kSelQ = 6;    // units in flight
+constexpr int kSelG = 4;    // tiles per unit
+
+// 16 KB of values per tile: 4096 four-byte or 2048 eight-byte elements.
+template <typename V>
+struct SelShape {
+    static constexpr int kTile = 16384 / static_cast<int>(sizeof(V));
+    static constexpr int kItems = kTile / kSelRole;  // per thread: 128 bytes of values
+    static constexpr int kEpc = 16 / static_cast<int>(sizeof(V));
+    static constexpr int kChunks = kItems / kEpc;
+};
+
+template <typename V>
+struct SelCtrl {
+    uint64_t rfull[kSelRS], rfree[kSelRS];
+    uint64_t sfull[kSelSS], sfree[kSelSS];
+    uint64_t uknown[kSelQ], ureduced[kSelQ], uprefix[kSelQ], ufree[kSelQ];
+    uint32_t r_tile[kSelRS];
+    uint32_t s_tile[kSelSS];
+    uint32_t unit_of[kSelQ];
+    uint32_t end_seq;
+    uint64_t uagg[kSelQ];
+    uint64_t upre[kSelQ];
+    uint32_t r_wtot[2][kSelWarps];
+    uint32_t tpre[kSelQ][kSelG][kSelRole];  // count before each thread within its unit
+    uint32_t ttot[kSelQ][kSelG];             // count of each tile
+};
+
+template <typename V>
+constexpr size_t sel_smem_bytes() {
+    constexpr size_t TILE = SelShape<V>::kTile;
+    return kSelRS * TILE + kSelSS * (TILE * sizeof(V) + TILE) + TILE * sizeof(V) + sizeof(SelCtrl<V>);
+}
+
+struct SelArgs {
+    const uint8_t* flags;
+};
+
+// Bit i set when byte i of the 4 * W bytes in w[] is non-zero.
+template <int W>
+__device__ __forceinline__ uint32_t nonzero_byte_mask(const uint32_t (&w)[W]) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+        // 0x01 in every non-zero byte, gathered into 4 bits by one multiply.
+        const uint32_t nz = __vcmpne4(w[j], 0u) & 0x01010101u;
+        m |= ((nz * 0x01020408u) >> 24) << (4 * j);
+    }
+    return m;
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a, const SelArgs sa) {
+    using Sh = SelShape<V>;
+    using D = DescTraits<uint64_t>;
+    using word = D::word;
+    constexpr int TILE = Sh::kTile;
+    constexpr int ITEMS = Sh::kItems;
+    constexpr int EPC = Sh::kEpc;
+    constexpr int CHUNKS = Sh::kChunks;
+    constexpr int FW = ITEMS / 4;  // flag words per thread
+    constexpr uint32_t kWarpLookback = 2, kWarpReduce = 2 + kSelLookback, kWarpFinal = kWarpReduce + kSelWarps;
+    constexpr int RS = kSelRS, SS = kSelSS, Q = kSelQ, G = kSelG;
+    static_assert(CHUNKS == 8, "128 bytes of values per thread");
+    static_assert(ITEMS <= 32, "one 32-bit mask of flags per thread");
+    using Ctrl = SelCtrl<V>;
+
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* rflags = smem_raw;
+    V* svals = reinterpret_cast<V*>(rflags + static_cast<size_t>(RS) * TILE);
+    uint8_t* sflags = reinterpret_cast<uint8_t*>(svals + static_cast<size_t>(SS) * TILE);
+    V* ostage = reinterpret_cast<V*>(sflags + static_cast<size_t>(SS) * TILE);
+    Ctrl* ctrl = reinterpret_cast<Ctrl*>(ostage + TILE);
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5;
+    const uint32_t lane = tid & 31u;
+    const uint32_t num_units = (a.num_tiles + G - 1) / G;
+
+    if (tid == 0) {
+        for (int s = 0; s < RS; ++s) {
+            ptx::mbar_init(&ctrl->rfull[s], 1);
+            ptx::mbar_init(&ctrl->rfree[s], kSelWarps);
+        }
+        for (int s = 0; s < SS; ++s) {
+            ptx::mbar_init(&ctrl->sfull[s], 1);
+            ptx::mbar_init(&ctrl->sfree[s], kSelWarps);
+        }
+        for (int q = 0; q < Q; ++q) {
+            ptx::mbar_init(&ctrl->uknown[q], 1);
+            ptx::mbar_init(&ctrl->ureduced[q], 1);
+            ptx::mbar_init(&ctrl->uprefix[q], 1);
+            ptx::mbar_init(&ctrl->ufree[q], kSelWarps);
+        }
+        ctrl->end_seq = 0xFFFFFFFFu;
+        ptx::fence_mbar_init();
+    }
+    __syncthreads();
+
+    const uint32_t epoch = ld_volatile_u32(&a.hdr->epoch);
+    const uint64_t long_budget = a.wait_budget_ns * 4 + 1000000000ull;
+    auto count_of = [&](uint32_t t) -> uint32_t { return t < a.num_tiles ? tile_count<TILE>(a.n, t) : 0u; };
+    auto wait1 = [&](uint64_t* bar, uint32_t ph, uint64_t b) -> bool {
+        return ptx::mbar_try_wait(bar, ph) || ptx::mbar_wait_bounded(bar, ph, ptx::global_timer_ns() + b);
+    };
+    // A thread's flags (logical order) as a bit mask; bytes past the 16-byte
+    // bulk part of a partial tile come from global memory.
+    auto flag_mask = [&](const uint8_t* stage, uint32_t t, uint32_t thr) -> uint32_t {
+        const uint32_t cnt = count_of(t);
+        uint32_t w[FW];
+        if (cnt == static_cast<uint32_t>(TILE)) {
+#pragma unroll
+            for (int j = 0; j < FW / 4; ++j) {
+                const uint4 q4 = *reinterpret_cast<const uint4*>(stage + thr * ITEMS + 16 * j);
+                w[4 * j] = q4.x;
+                w[4 * j + 1] = q4.y;
+                w[4 * j + 2] = q4.z;
+                w[4 * j + 3] = q4.w;
+            }
+        } else {
+            const uint32_t bulk = cnt & ~15u;
+            const uint8_t* g = sa.flags + static_cast<uint64_t>(t) * TILE;
+#pragma unroll
+            for (int j = 0; j < FW; ++j) {
+                uint32_t x = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const uint32_t i = thr * ITEMS + 4 * j + b;
+                    const uint32_t byte = i < bulk ? stage[i] : (i < cnt ? g[i] : 0u);
+                    x |= (byte ? 1u : 0u) << (8 * b);
+                }
+                w[j] = x;
+            }
+        }
+        return nonzero_byte_mask<FW>(w);
+    };
+
+    // ======================================================== R-loader
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint64_t pol = ptx::policy_evict_last();
+            bool stop = false;
+            uint32_t rn = 0;
+            bool ok = true;
+            for (uint32_t i = 0; ok; ++i) {
+                const int q = static_cast<int>(i % Q);
+                if (i >= Q && !wait1(&ctrl->ufree[q], ((i - Q) / Q) & 1u, long_budget)) break;
+                uint32_t u = kTileEnd;
+                if (!stop) {
+                    const uint32_t raw = atomicAdd(&a.hdr->tile_counter, 1u);
+                    if (raw < num_units && ld_volatile_u32(&a.hdr->error_flags) == 0)
+                        u = raw;
+                    else
+                        stop = true;
+                }
+                ctrl->unit_of[q] = u;
+                ptx::mbar_arrive(&ctrl->uknown[q]);
+                if (u == kTileEnd) {
+                    for (uint32_t m = 1; m < static_cast<uint32_t>(kSelLookback) && ok; ++m) {
+                        const uint32_t i2 = i + m;
+                        const int q2 = static_cast<int>(i2 % Q);
+                        if (i2 >= Q && !wait1(&ctrl->ufree[q2], ((i2 - Q) / Q) & 1u, long_budget)) ok = false;
+                        if (ok) {
+                            ctrl->unit_of[q2] = kTileEnd;
+                            ptx::mbar_arrive(&ctrl->uknown[q2]);
+                        }
+                    }
+                    const int s = static_cast<int>(rn % RS);
+                    if (ok && (rn < RS || wait1(&ctrl->rfree[s], ((rn - RS) / RS) & 1u, long_budget))) {
+                        ctrl->r_tile[s] = kTileEnd;
+                        ptx::mbar_arrive(&ctrl->rfull[s]);
+                    }
+                    break;
+                }
+                for (int k = 0; k < G && ok; ++k, ++rn) {
+                    const int s = static_cast<int>(rn % RS);
+                    if (rn >= RS && !wait1(&ctrl->rfree[s], ((rn - RS) / RS) & 1u, long_budget)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t t = u * G + k;
+                    ctrl->r_tile[s] = t;
+                    const uint32_t bytes = count_of(t) & ~15u;
+                    ptx::mbar_arrive_expect_tx(&ctrl->rfull[s], bytes);
+                    if (bytes)
+                        ptx::bulk_load_hint(rflags + static_cast<size_t>(s) * TILE,
+                                            sa.flags + static_cast<uint64_t>(t) * TILE, bytes, &ctrl->rfull[s], pol);
+                }
+            }
+            if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
+        }
+    }
+    // ======================================================== S-loader
+    else if (warp == 1) {
+        if (lane == 0) {
+            const uint64_t pol = ptx::policy_evict_first();
+            uint32_t sn = 0;
+            bool ok = true;
+            for (uint32_t i = 0; ok; ++i) {
+                const int q = static_cast<int>(i % Q);
+                if (!wait1(&ctrl->uknown[q], (i / Q) & 1u, long_budget)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t u = ctrl->unit_of[q];
+                const bool end = u == kTileEnd;
+                // One unit ahead of the prefix (see scan_l2.cuh).
+                if (!end && i >= 1) {
+                    const uint32_t ip = i - 1;
+                    bool ready = false;
+                    const uint64_t deadline = ptx::global_timer_ns() + long_budget;
+                    while (!(ready = ptx::mbar_try_wait(&ctrl->uprefix[ip % Q], (ip / Q) & 1u))) {
+                        if (ld_volatile_u32(&ctrl->end_seq) <= ip || ptx::global_timer_ns() > deadline) break;
+                    }
+                    if (!ready) {
+                        ok = false;
+                        break;
+                    }
+                }
+                for (int k = 0; k < (end ? 1 : G); ++k, ++sn) {
+                    const int s = static_cast<int>(sn % SS);
+                    if (sn >= SS && !wait1(&ctrl->sfree[s], ((sn - SS) / SS) & 1u, long_budget)) {
+                        ok = false;
+                        break;
+                    }
+                    if (end) {
+                        ctrl->s_tile[s] = kTileEnd;
+                        ptx::mbar_arrive(&ctrl->sfull[s]);
+                        break;
+                    }
+                    const uint32_t t = u * G + k;
+                    ctrl->s_tile[s] = t;
+                    const uint32_t cnt = count_of(t);
+                    const uint32_t vbytes = (cnt * static_cast<uint32_t>(sizeof(V))) & ~15u;
+                    const uint32_t fbytes = cnt & ~15u;
+                    ptx::mbar_arrive_expect_tx(&ctrl->sfull[s], vbytes + fbytes);
+                    if (vbytes)
+                        ptx::bulk_load_hint(svals + static_cast<size_t>(s) * TILE,
+                                            static_cast<const V*>(a.in) + static_cast<uint64_t>(t) * TILE, vbytes,
+                                            &ctrl->sfull[s], pol);
+                    if (fbytes)
+                        ptx::bulk_load_hint(sflags + static_cast<size_t>(s) * TILE,
+                                            sa.flags + static_cast<uint64_t>(t) * TILE, fbytes, &ctrl->sfull[s], pol);
+                }
+                if (end) break;
+            }
+            if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
+        }
+    }
+    // ======================================================== lookback
+    else if (warp < kWarpReduce) {
+        word* desc = static_cast<word*>(a.desc);
+        int64_t own_prev = -1;
+        uint64_t own_incl = 0;
+        for (uint32_t i = warp - kWarpLookback;; i += kSelLookback) {
+            const int q = static_cast<int>(i % Q);
+            const uint32_t ph = (i / Q) & 1u;
+            bool ok = true;
+            if (lane == 0) ok = wait1(&ctrl->uknown[q], ph, long_budget);
+            ok = __shfl_sync(kFullMask, ok, 0);
+            __syncwarp();
+            if (!ok) {
+                if (lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
+                break;
+            }
+            const uint32_t u = ctrl->unit_of[q];
+            if (u == kTileEnd) break;
+            const uint64_t pre =
+                u == 0 ? 0ull : lookback<uint64_t, TILE * G, false>(a, u, epoch, lane, 0ull, own_prev, own_incl);
+            uint32_t state = 0;  // 0 reduced, 1 reduce warps stopped, 2 timeout
+            if (lane == 0) {
+                const uint64_t deadline = ptx::global_timer_ns() + long_budget;
+                while (!ptx::mbar_try_wait(&ctrl->ureduced[q], ph)) {
+                    if (ld_volatile_u32(&ctrl->end_seq) <= i) {
+                        state = 1;
+                        break;
+                    }
+                    if (ptx::global_timer_ns() > deadline) {
+                        state = 2;
+                        break;
+                    }
+                }
+            }
+            state = __shfl_sync(kFullMask, state, 0);
+            __syncwarp();
+            if (state != 0) {
+                if (lane == 0 && state == 2) raise_error(a.hdr, kErrPipelineTimeout);
+                break;
+            }
+            const uint64_t incl = pre + ctrl->uagg[q];
+            if (lane == 0) {
+                if (u != 0) D::store(desc + u, D::pack(kInclusive, epoch, incl));
+                if (u == num_units - 1 && a.carry_out != nullptr) *static_cast<uint64_t*>(a.carry_out) = incl;
+                ctrl->upre[q] = pre;
+                ptx::mbar_arrive(&ctrl->uprefix[q]);
+            }
+            own_prev = u;
+            own_incl = incl;
+            __syncwarp();
+        }
+    }
+    // ======================================================== reduce
+    else if (warp < kWarpFinal) {
+        const uint32_t r = tid - kWarpReduce * 32;
+        const uint32_t rw = warp - kWarpReduce;
+        word* desc = static_cast<word*>(a.desc);
+        uint32_t unit_cnt = 0;
+        for (uint32_t rn = 0;; ++rn) {
+            const int s = static_cast<int>(rn % RS);
+            const uint32_t i = rn / G;
+            const int k = static_cast<int>(rn % G);
+            const int q = static_cast<int>(i % Q);
+            const bool ok = wait1(&ctrl->rfull[s], (rn / RS) & 1u, long_budget);
+            const uint32_t t = ok ? ctrl->r_tile[s] : kTileEnd;
+            const bool live = t != kTileEnd;
+            const uint32_t cnt = live ? static_cast<uint32_t>(__popc(flag_mask(rflags + static_cast<size_t>(s) * TILE,
+                                                                               t, r)))
+                                      : 0u;
+            const uint32_t winc = warp_inclusive_scan(cnt, lane);
+            if (lane == 31) ctrl->r_wtot[rn & 1u][rw] = winc;
+            const bool stop = named_bar_or(1, kSelRole, !live || !ok);
+            if (lane == 0 && live) ptx::mbar_arrive(&ctrl->rfree[s]);
+            if (stop) {
+                if (r == 0) {
+                    if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
+                    *reinterpret_cast<volatile uint32_t*>(&ctrl->end_seq) = i;
+                }
+                break;
+            }
+            uint32_t wpre = 0, tot = 0;
+#pragma unroll
+            for (int w2 = 0; w2 < kSelWarps; ++w2) {
+                const uint32_t x = ctrl->r_wtot[rn & 1u][w2];
+                wpre += static_cast<uint32_t>(w2) < rw ? x : 0u;
+                tot += x;
+            }
+            ctrl->tpre[q][k][r] = unit_cnt + wpre + (winc - cnt);
+            if (r == 0) ctrl->ttot[q][k] = tot;
+            unit_cnt += tot;
+            if (k == G - 1) {
+                if (r == 0) {
+                    const uint32_t u = t / G;
+                    D::store(desc + u, D::pack(u == 0 ? kInclusive : kAggregate, epoch, unit_cnt));
+                    ctrl->uagg[q] = unit_cnt;
+                    ptx::mbar_arrive(&ctrl->ureduced[q]);
+                }
+                unit_cnt = 0;
+            }
+        }
+    }
+    // ======================================================== finalize
+    else {
+        const uint32_t f = tid - kWarpFinal * 32;
+        const uint32_t rot = f & 7u;
+        uint64_t run = 0;  // the unit's output position
+        for (uint32_t sn = 0;; ++sn) {
+            const int s = static_cast<int>(sn % SS);
+            const uint32_t i = sn / G;
+            const int k = static_cast<int>(sn % G);
+            const int q = static_cast<int>(i % Q);
+            const bool ok = wait1(&ctrl->sfull[s], (sn / SS) & 1u, long_budget);
+            const uint32_t t = ok ? ctrl->s_tile[s] : kTileEnd;
+            // All finalize threads stop together (the end, or a wait that ran
+            // out anywhere): the staging barriers below then never strand a
+            // warp.
+            if (named_bar_or(3, kSelRole, t == kTileEnd)) {
+                if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
+                break;
+            }
+            const V* vb = svals + static_cast<size_t>(s) * TILE;
+            const uint32_t cnt = count_of(t);
+            const bool full_tile = cnt == static_cast<uint32_t>(TILE);
+            V v[ITEMS];
+            if (full_tile) {
+#pragma unroll
+                for (int c8 = 0; c8 < CHUNKS; ++c8) {
+                    const uint32_t c = (c8 + rot) & (CHUNKS - 1);
+                    const Chunk<V> qv = *reinterpret_cast<const Chunk<V>*>(vb + f * ITEMS + c * EPC);
+#pragma unroll
+                    for (int e = 0; e < EPC; ++e) v[c8 * EPC + e] = qv.v[e];
+                }
+            } else {
+                const uint32_t bulk = ((cnt * static_cast<uint32_t>(sizeof(V))) & ~15u) / sizeof(V);
+                const V* g = static_cast<const V*>(a.in) + static_cast<uint64_t>(t) * TILE;
+#pragma unroll
+                for (int e = 0; e < ITEMS; ++e) {
+                    const uint32_t li = f * ITEMS + e;
+                    v[e] = li < bulk ? vb[li] : (li < cnt ? g[li] : V(0));
+                }
+            }
+            const uint32_t mask = flag_mask(sflags + static_cast<size_t>(s) * TILE, t, f);
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&ctrl->sfree[s]);  // this warp is done with the stage
+            if (k == 0) {
+                bool pok = wait1(&ctrl->uprefix[q], (i / Q) & 1u, long_budget);
+                pok = __all_sync(kFullMask, pok);
+                if (!pok && lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
+                run = ctrl->upre[q];
+            }
+            // Selected items of each register chunk, and where each chunk's
+            // run starts in logical order within the thread.
+            const uint32_t rrot = full_tile ? rot : 0u;
+            uint32_t cs[CHUNKS];
+#pragma unroll
+            for (int c8 = 0; c8 < CHUNKS; ++c8) {
+                const uint32_t l = (c8 + rrot) & (CHUNKS - 1);
+                cs[c8] = static_cast<uint32_t>(__popc((mask >> (l * EPC)) & ((1u << EPC) - 1u)));
+            }
+            uint32_t cpre[CHUNKS];
+            uint32_t total;
+            rotated_chunk_prefix<uint32_t, CHUNKS>(cs, rrot, cpre, total);
+            const uint32_t tile_base = ctrl->tpre[q][k][0];
+            const uint32_t mine = ctrl->tpre[q][k][f] - tile_base;
+            const uint32_t tile_cnt = ctrl->ttot[q][k];
+            // The staging tile may still be read by the previous copy-out.
+            ptx::named_bar_sync(2, kSelRole);
+#pragma unroll
+            for (int c8 = 0; c8 < CHUNKS; ++c8) {
+                const uint32_t l = (c8 + rrot) & (CHUNKS - 1);
+                uint32_t pos = mine + cpre[c8];
+#pragma unroll
+                for (int e = 0; e < EPC; ++e) {
+                    if ((mask >> (l * EPC + e)) & 1u) ostage[pos++] = v[c8 * EPC + e];
+                }
+            }
+            ptx::named_bar_sync(2, kSelRole);
+            V* out = static_cast<V*>(a.out) + run + tile_base;
+            for (uint32_t x = f; x < tile_cnt; x += kSelRole) out[x] = ostage[x];
+            if (k == G - 1 && lane == 0) ptx::mbar_arrive(&ctrl->ufree[q]);
+        }
+    }
+
+    // Last CTA out: return the counters to zero and advance the epoch (every
+    // 2^30 launches, clear the descriptors first), so that the next launch
+    // needs no memset and the launch replays from a CUDA graph.
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        const uint32_t prev = atomicAdd(&a.hdr->exit_counter, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            a.hdr->tile_counter = 0;
+            a.hdr->exit_counter = 0;
+            uint32_t e = epoch + 1;
+            if ((e & kEpochMask) == 0) {
+                word* desc = static_cast<word*>(a.desc);
+                for (unsigned long long q = 0; q < a.hdr->capacity_tiles; ++q) D::store(desc + q, D::zero());
+                e += 1;
+            }
+            __threadfence();
+            a.hdr->epoch = e;
+        }
+    }
+}
+
+template <typename V>
+cudaError_t launch_select_t(const ScanArgs& a, const SelArgs& sa, int num_sms, cudaStream_t stream,
+                            LaunchInfo* info) {
+    auto kern = select_kernel<V>;
+    constexpr size_t smem = sel_smem_bytes<V>();
+    static_assert(smem <= 232448, "227 KB of shared memory per CTA");
+    int occ = 0;
+    cudaError_t err = resident_ctas_per_sm(kern, kSelThreads, smem, &occ);
+    if (err != cudaSuccess) return err;
+    const uint32_t units = (a.num_tiles + kSelG - 1) / kSelG;
+    const int grid = persistent_grid(units, occ, num_sms);
+    if (info) *info = LaunchInfo{grid, kSelThreads, smem};
+    kern<<<grid, kSelThreads, smem, stream>>>(a, sa);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+uint32_t select_tile_elems(size_t elem_size) { return elem_size == 8 ? 2048u : 4096u; }
+
+cudaError_t launch_select(size_t elem_size, const ScanArgs& a, const uint8_t* flags, int num_sms, cudaStream_t stream,
+                          LaunchInfo* info) {
+    const SelArgs sa{flags};
+    return elem_size == 8 ? launch_select_t<uint64_t>(a, sa, num_sms, stream, info)
+                          : launch_select_t<uint32_t>(a, sa, num_sms, stream, info);
+}
+
+}  // namespace gps

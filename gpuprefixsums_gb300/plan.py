@@ -103,6 +103,26 @@ class Plan:
                                      ctypes.c_void_p(_stream_handle(stream))), "gps_scan_segmented")
         return out
 
+    def select(self, x, flags, out=None, num_selected=None, stream=None):
+        """Stream compaction: the elements of CUDA tensor x whose flag byte
+        (uint8/bool CUDA tensor, same length) is non-zero, in order, into
+        out[:count]; count (int64 CUDA tensor of one element) is written on
+        the device. Returns (out, num_selected)."""
+        import torch
+        if x.element_size() != self.elem_size or not (x.is_cuda and x.is_contiguous()):
+            raise ValueError("x must be a contiguous CUDA tensor with the plan's element size")
+        if flags.element_size() != 1 or flags.numel() != x.numel() or not (flags.is_cuda and flags.is_contiguous()):
+            raise ValueError("flags must be a contiguous one-byte CUDA tensor as long as x")
+        if out is None:
+            out = torch.empty_like(x)
+        if num_selected is None:
+            num_selected = torch.zeros(1, dtype=torch.int64, device=x.device)
+        check(lib.gps_select_flagged(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(flags.data_ptr()),
+                                     ctypes.c_void_p(out.data_ptr()), x.numel(),
+                                     ctypes.c_void_p(num_selected.data_ptr()), ctypes.c_void_p(_stream_handle(stream))),
+              "gps_select_flagged")
+        return out, num_selected
+
     def autotune(self, x, offsets=None, out=None, inclusive: bool = False, stream=None) -> dict:
         """Times the generic kernel's launch configurations on these tensors
         (batched when offsets is given) and keeps the fastest for the size

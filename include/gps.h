@@ -129,6 +129,19 @@ gps_status gps_scan(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d
 gps_status gps_scan_segmented(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
                               const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream);
 
+/* Stream compaction (select by flags): copies the elements d_in[i] whose
+ * flag byte d_flags[i] is non-zero, in their order, to d_out[0 .. count), and
+ * writes count to *d_num_selected (uint64, device memory). One launch: the
+ * flag scan is fused with the scatter, so the values and flags are read once
+ * and only the selected values are written. Any GPS_ALGO_CSDL plan; the
+ * element size is the plan's (4 bytes for u32 / f32, 8 for u64). d_in and
+ * d_flags 16-byte aligned, d_out aligned to the element size and not
+ * overlapping them; n <= max_n. Asynchronous on `stream`; capturable.
+ * No counterpart in the reference; it is the scan's next consumer (the
+ * exclusive scan of the flags gives each selected element's output index). */
+gps_status gps_select_flagged(gps_plan plan, const void* d_in, const uint8_t* d_flags, void* d_out, uint64_t n,
+                              uint64_t* d_num_selected, gps_stream_t stream);
+
 /* Autotuner of the batched / floating-point kernel. Times each launch
  * configuration it knows -- tiles per lookback unit (1 or 4 tiles of 4096
  * 4-byte or 2048 8-byte elements) times CTA count (one per SM, or half) -- on

@@ -40,6 +40,7 @@ def lib() -> ctypes.CDLL:
             ("oracle_scan_u32_mt", [P, P, U64, I, I], I),
             ("oracle_scan_f32_exact", [P, P, U64, I], None),
             ("oracle_scan_f32_serial", [P, P, U64, I], None),
+            ("oracle_select", [P, P, P, U64, I], U64),
             ("oracle_version", [], I),
         ]:
             fn = getattr(L, name)
@@ -123,3 +124,12 @@ def scan_f32_serial(x: np.ndarray, inclusive: bool = True) -> np.ndarray:
     out = np.empty_like(x)
     lib().oracle_scan_f32_serial(_ptr(x), _ptr(out), x.size, int(inclusive))
     return out
+
+
+def select(x: np.ndarray, flags: np.ndarray) -> np.ndarray:
+    """Stream compaction: the elements of x whose flag byte is non-zero."""
+    x = np.ascontiguousarray(x)
+    flags = np.ascontiguousarray(flags, dtype=np.uint8)
+    out = np.empty_like(x)
+    count = lib().oracle_select(_ptr(x), _ptr(flags), _ptr(out), x.size, x.itemsize)
+    return out[:count]

@@ -349,4 +349,20 @@ void oracle_scan_f32_serial(const float* in, float* out, uint64_t n, int inclusi
     }
 }
 
+/* Stream compaction: out[j] = the j-th in[i] with flags[i] != 0, by an
+ * exclusive scan of the flags done inline (the output index of a selected
+ * element is the number of selected elements before it). Returns the count.
+ * Element size 4 or 8 bytes. */
+uint64_t oracle_select(const void* in, const uint8_t* flags, void* out, uint64_t n, int elem_size) {
+    uint64_t j = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (flags[i] != 0) {
+            memcpy((uint8_t*)out + j * (uint64_t)elem_size, (const uint8_t*)in + i * (uint64_t)elem_size,
+                   (size_t)elem_size);
+            ++j;
+        }
+    }
+    return j;
+}
+
 int oracle_version(void) { return 1; }

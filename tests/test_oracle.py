@@ -138,3 +138,12 @@ def test_exact_fp32_prefix_is_correctly_rounded():
         assert got[i] == float(acc), i
     exc = oracle.scan_f32_exact(x[:10], inclusive=False)
     assert exc[0] == 0.0 and exc[1] == float(x[0])
+
+
+def test_select_matches_boolean_indexing():
+    rng = np.random.default_rng(9)
+    for dtype in (np.uint32, np.uint64):
+        x = rng.integers(0, 2 ** 31, size=10_001).astype(dtype)
+        flags = (rng.random(x.size) < 0.3).astype(np.uint8) * rng.integers(1, 256, size=x.size).astype(np.uint8)
+        assert np.array_equal(oracle.select(x, flags), x[flags != 0])
+    assert oracle.select(np.zeros(0, np.uint32), np.zeros(0, np.uint8)).size == 0
