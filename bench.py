@@ -577,6 +577,16 @@ def run_ours(args, world, rank, local):
             o_ms = time_loop(lambda: p2.scan(d_in, d_out, stream=stream), reps, stream)
             p2.check(stream)
         compare[f"{other}_gbs"] = round(alg_bytes / (o_ms * 1e-3) / 1e9, 2)
+        if args.algo == "csdl":
+            # The same chained scan with the decoupled fallback on (a
+            # predecessor silent for 4 polls is re-reduced by its successor).
+            with Plan("csdl", "u32", max_n=n) as p3:
+                p3.set_fallback(4)
+                for _ in range(3):
+                    p3.scan(d_in, d_out, stream=stream)
+                f_ms = time_loop(lambda: p3.scan(d_in, d_out, stream=stream), reps, stream)
+                p3.check(stream)
+            compare["csdl_fallback_gbs"] = round(alg_bytes / (f_ms * 1e-3) / 1e9, 2)
 
         # End to end through the C ABI from pinned host memory.
         h_in = torch.empty(n, dtype=torch.int32, pin_memory=True)

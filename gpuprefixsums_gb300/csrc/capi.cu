@@ -143,7 +143,8 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
         err = launch_generic(p->dtype, inclusive, a, nullptr, generic_config(p, false, n), p->num_sms, stream,
                              &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
-        err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0, a, p->num_sms, stream, &p->last_launch);
+        err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0 || p->stall.fallback_polls != 0, a, p->num_sms,
+                               stream, &p->last_launch);
     } else {
         err = gps::launch_rts(p->dtype, inclusive, a, p->area, p->num_sms, stream, &p->last_launch);
     }
@@ -578,6 +579,14 @@ gps_status gps_plan_set_stall(gps_plan p, uint32_t mode, uint32_t period, uint32
     if (mode != 0 && period == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "period must be positive");
     if (delay_ns > 1000000000u) return fail(GPS_ERR_INVALID_ARGUMENT, "delay %u ns exceeds one second", delay_ns);
     p->stall = gps::StallConfig{mode, period, seed, delay_ns, fallback_polls, 0};
+    return GPS_OK;
+}
+
+gps_status gps_plan_set_fallback(gps_plan p, uint32_t fallback_polls) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (fallback_polls != 0 && p->algo != GPS_ALGO_CSDL)
+        return fail(GPS_ERR_UNSUPPORTED, "the decoupled fallback applies to the chained scan only");
+    p->stall = gps::StallConfig{0, 1, 0, 0, fallback_polls, 0};
     return GPS_OK;
 }
 

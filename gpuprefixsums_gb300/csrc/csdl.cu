@@ -79,7 +79,9 @@ cudaError_t dispatch_csdl(bool inclusive, bool stall, const ScanArgs& a, int num
         return inclusive ? launch_l2_t<T, true, false>(a, num_sms, stream, info)
                          : launch_l2_t<T, false, false>(a, num_sms, stream, info);
     }
-    if (stall) return cudaErrorInvalidValue;  // test mode wants aligned buffers
+    // The forced-stall test mode wants aligned buffers; the fallback alone
+    // (stall mode 0) is a robustness option the ring kernel runs without.
+    if (stall && a.stall.mode != 0) return cudaErrorInvalidValue;
     return inclusive ? launch_csdl_t<T, true, false, false>(a, num_sms, stream, info)
                      : launch_csdl_t<T, false, false, false>(a, num_sms, stream, info);
 }

@@ -278,7 +278,7 @@ __device__ T lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t la
             // Not resolvable yet: the slot at position `gap` is not ready.
             ++polls;
             if (STALL) {
-                if (lane == 0) atomicAdd(&a.hdr->stat_polls, 1ull);
+                if (lane == 0 && a.stall.mode != 0) atomicAdd(&a.hdr->stat_polls, 1ull);
                 if (a.stall.fallback_polls != 0 && polls >= a.stall.fallback_polls) {
                     // Re-reduce the nearest predecessor that is still not ready
                     // and try to insert its aggregate.

@@ -168,6 +168,11 @@ class Plan:
     def set_stall(self, mode: int, period: int = 8, seed: int = 0, delay_ns: int = 0, fallback_polls: int = 0) -> None:
         check(lib.gps_plan_set_stall(self._h, mode, period, seed, delay_ns, fallback_polls), "gps_plan_set_stall")
 
+    def set_fallback(self, fallback_polls: int) -> None:
+        """Decoupled fallback: re-reduce a predecessor that shows no progress
+        for this many lookback polls (0: off)."""
+        check(lib.gps_plan_set_fallback(self._h, int(fallback_polls)), "gps_plan_set_fallback")
+
     def stats(self, stream=None) -> dict:
         s = _lib.LookbackStats()
         check(lib.gps_plan_stats(self._h, ctypes.c_void_p(_stream_handle(stream)), ctypes.byref(s)), "gps_plan_stats")

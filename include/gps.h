@@ -201,6 +201,20 @@ gps_status gps_plan_set_wait_budget(gps_plan plan, uint64_t budget_ns);
 gps_status gps_plan_set_stall(gps_plan plan, uint32_t mode, uint32_t period, uint32_t seed,
                               uint32_t delay_ns, uint32_t fallback_polls);
 
+/* Decoupled fallback (production form of the mode above, without forced
+ * stalls): a chained-scan lookback that sees no progress on a predecessor
+ * for fallback_polls polls re-reduces that predecessor's input itself and
+ * inserts the aggregate with a compare-and-swap, instead of waiting on. This
+ * makes the scan independent of the scheduling of other CTAs, at the price
+ * of re-reading a slow predecessor's input. 0 turns it off (default).
+ * Integer chained-scan plans (u32, u64); batched, floating-point and select
+ * launches do not use it, nor does a scan of unaligned buffers.
+ * Replaces: the reference's Chained Scan with Decoupled Lookback and
+ * Decoupled Fallback (README.md:9-13;
+ * GPUPrefixSumsD3D12/Shaders/ChainedScanDecoupledLookbackDecoupledFallback.hlsl:81-164),
+ * which the CUDA part only shows in its EmulatedDeadlocking test. */
+gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
+
 /* Lookback statistics gathered while forced-stall mode is on. Synchronizes
  * `stream`. */
 typedef struct gps_lookback_stats {

@@ -236,6 +236,30 @@ def test_forced_stall_reference_pattern_with_fallback(cuda, dtype):
     assert st["fallbacks"] > 0 and st["inserts"] > 0
 
 
+@pytest.mark.parametrize("dtype", ["u32", "u64"])
+def test_decoupled_fallback_mode_is_exact(cuda, dtype):
+    # Production fallback (no forced stalls): aggressive re-reduction after a
+    # single empty poll, in and out of place, aligned and unaligned buffers.
+    for n in (1, 4097, 50 * TILE[dtype] + 3, 1 << 22):
+        x = rand(dtype, n, seed=n)
+        want = oracle.scan(x, inclusive=False)
+        with Plan("csdl", dtype, max_n=n + 4) as plan:
+            plan.set_fallback(1)
+            d = to_dev(x)
+            out = plan.scan(d, inclusive=False)
+            plan.scan(d, out=d, inclusive=False)  # in place
+            plan.check()
+            assert np.array_equal(to_host(out, NP[dtype]), want), n
+            assert np.array_equal(to_host(d, NP[dtype]), want), n
+            if n > 2:
+                buf = to_dev(np.concatenate([x[:1], x]))  # element-aligned, not 16-byte aligned
+                un = buf[1:]
+                res = plan.scan(un, out=un, inclusive=False)
+                plan.check()
+                assert np.array_equal(to_host(res, NP[dtype]), want), n
+            plan.set_fallback(0)
+
+
 @pytest.mark.parametrize("inclusive", [False, True])
 def test_forced_stall_seeded_delays_without_fallback(cuda, inclusive):
     # Seeded random tiles are delayed by 30 us; successors just wait.
