@@ -18,6 +18,7 @@ Reported (one JSON line on rank 0):
   compare      D2D copy of the same bytes (the 100% line), CUB DeviceScan and
                the reduce-then-scan path on the same buffers;
   cpu_baseline the oracle's serial scan on one host core;
+  sweep        the chained scan by size (2^10 .. 2^28 u32) and u64 at 2^27;
   batched      4096 independent u32 exclusive scans, lengths log-uniform in
                [1, 2^20] (seeded), CSR offsets: one autotuned launch replayed
                from a CUDA graph against a graph of one plain scan per segment
@@ -349,6 +350,36 @@ def run_select(stream, copy_gbs, reps=20):
     return res
 
 
+def run_sweep(stream, d_in, d_out):
+    """Config-2 sizes: u32 exclusive chained scan at n = 2^10 .. 2^28 (every
+    second power of two) on the benchmark's buffers, and u64 at n = 2^27.
+    Inputs below about 2^24 elements stay in L2 between launches."""
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    res = {"workload": "u32 exclusive chained scan by size (L2-resident below ~2^24), u64 exclusive at 2^27",
+           "u32_gbs": {}}
+    with Plan("csdl", "u32", max_n=d_in.numel()) as plan:
+        for k in range(10, 29, 2):
+            n = 1 << k
+            step = lambda: plan.scan(d_in, d_out, n=n, stream=stream)  # noqa: E731
+            for _ in range(3):
+                step()
+            ms = time_loop(step, max(20, min(2000, (1 << 30) // n)), stream)
+            res["u32_gbs"][f"2^{k}"] = {"gbs": round(n * 8 / (ms * 1e-3) / 1e9, 2), "us": round(ms * 1e3, 2)}
+        plan.check(stream)
+    n64 = 1 << 27
+    x64, o64 = d_in.view(torch.int64)[:n64], d_out.view(torch.int64)[:n64]
+    with Plan("csdl", "u64", max_n=n64) as plan:
+        step = lambda: plan.scan(x64, o64, stream=stream)  # noqa: E731
+        for _ in range(3):
+            step()
+        ms = time_loop(step, 50, stream)
+        plan.check(stream)
+    res["u64_2^27_gbs"] = round(n64 * 16 / (ms * 1e-3) / 1e9, 2)
+    return res
+
+
 def fp_errors_vs_f64(got, ref):
     """max / median relative prefix error (nonzero reference prefixes) and
     relative error of the final sum, against a float64 scan."""
@@ -605,6 +636,7 @@ def run_ours(args, world, rank, local):
                "path": "gps_scan_host: pinned host -> device -> host, chunked and overlapped"}
 
         if not args.no_extras:
+            extras["sweep"] = run_sweep(stream, d_in, d_out)
             extras["batched"] = run_batched(stream, compare.get("d2d_copy_gbs"))
             extras["fp32"] = run_fp32(stream)
             extras["mixed"] = run_mixed(stream, compare.get("d2d_copy_gbs"))
