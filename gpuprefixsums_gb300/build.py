@@ -127,6 +127,29 @@ def build_compat_selftest(force: bool = False) -> str:
     return SELFTEST_BIN
 
 
+DEVTEST_SRC = os.path.join(os.path.dirname(PKG_DIR), "tests", "device", "primitives_test.cu")
+DEVTEST_LIB = os.path.join(BUILD_DIR, "libgps_devtest.so")
+
+
+def build_device_tests(force: bool = False) -> str:
+    """Build the test kernels of include/gps_device.cuh (the device-callable
+    primitives) into _build/libgps_devtest.so."""
+    deps = [DEVTEST_SRC, os.path.join(INCLUDE_DIR, "gps_device.cuh")]
+    if not force and os.path.exists(DEVTEST_LIB) and \
+            os.path.getmtime(DEVTEST_LIB) >= max(os.path.getmtime(d) for d in deps):
+        return DEVTEST_LIB
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = DEVTEST_LIB + ".tmp"
+    cmd = [nvcc_path(), *ARCH_FLAGS, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-cudart", "shared",
+           "-I", INCLUDE_DIR, "-o", tmp, DEVTEST_SRC,
+           "-Xlinker", "-rpath", "-Xlinker", os.path.join(cuda_home(), "lib64")]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"device primitive tests build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, DEVTEST_LIB)
+    return DEVTEST_LIB
+
+
 if __name__ == "__main__":
     print(build_library(force=True))
     print(build_compat_selftest(force=True))
