@@ -67,9 +67,10 @@ def parse_args():
     p.add_argument("--no-compare", action="store_true",
                    help="only the timed scans (for profiling): no copy/CUB/RTS/e2e/CPU legs")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, fp32 and mixed workloads")
-    p.add_argument("--profile-case", choices=["batched", "f32c"], default=None,
-                   help="launch one small case of a generic-kernel workload three times and exit (ncu captures): "
-                        "1024 of the batched workload's segments, or 2^26 compensated-f32 elements")
+    p.add_argument("--profile-case", choices=["batched", "f32c", "select"], default=None,
+                   help="launch one small case three times and exit (ncu captures): 1024 of the batched "
+                        "workload's segments, 2^26 compensated-f32 elements, or a select of 2^26 u32 by "
+                        "Bernoulli(0.3) flags")
     p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
@@ -704,6 +705,15 @@ def run_profile_case(args):
             for _ in range(3):
                 out = plan.scan_segmented(x, d_off)
             plan.check()
+    elif args.profile_case == "select":
+        n = 1 << 26
+        x = torch.randint(-2 ** 31, 2 ** 31 - 1, (n,), dtype=torch.int32, device="cuda")
+        fl = (torch.rand(n, device="cuda") < 0.3).to(torch.uint8)
+        with Plan("csdl", "u32", max_n=n) as plan:
+            for _ in range(3):
+                out, cnt = plan.select(x, fl)
+            plan.check()
+        out = out[:int(cnt.item())]
     else:
         n = 1 << 26
         x = torch.randn(n, device="cuda")
