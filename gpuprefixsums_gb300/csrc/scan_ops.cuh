@@ -36,12 +36,14 @@ __device__ __forceinline__ float shfl_up_any(float s, uint32_t d) { return __shf
 // kL2Prefetch: the kernel prefetches each unit into L2 when it takes the
 // unit (pays off for the streaming-bound operations, measured 3-4% on GB300;
 // the compensated scan is bound by its arithmetic and loses 4% instead).
+// kSplit: threads per 128-byte row of a tile (1: 4 + 4 compute warps).
 template <typename U>
 struct OpInt {
     using T = U;
     using S = U;
     using C = U;
     static constexpr bool kL2Prefetch = true;
+    static constexpr int kSplit = 1;
     __device__ static S zero() { return 0; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
@@ -70,6 +72,7 @@ struct OpF32 {
     using S = float;
     using C = float;
     static constexpr bool kL2Prefetch = true;
+    static constexpr int kSplit = 1;
     __device__ static S zero() { return 0.0f; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
@@ -110,6 +113,10 @@ struct OpF32C {
     using S = F2;
     using C = double;
     static constexpr bool kL2Prefetch = false;
+    // One thread per 128-byte row. (Two per row -- 8 reduce and 8 finalize
+    // warps of 16 items -- measured 25% slower on GB300: the per-thread
+    // prefixes double and leave room for fewer stages.)
+    static constexpr int kSplit = 1;
     __device__ static S zero() { return F2{0.0f, 0.0f}; }
     __device__ static S lift(T x) { return F2{x, 0.0f}; }
     __device__ static S add(S a, S b) {

@@ -186,7 +186,7 @@ template <class Op, int RW, int RS, int SS, int Q, int G, bool SEG>
 struct SegCtrl {
     using S = typename Op::S;
     using C = typename Op::C;
-    static constexpr int kHeadWords = TileShape<typename Op::T, RW>::kTile / 32;
+    static constexpr int kHeadWords = 16384 / static_cast<int>(sizeof(typename Op::T)) / 32;
     uint64_t rfull[RS], rfree[RS];
     uint64_t sfull[SS], sdone[SS], sfree[SS];
     uint64_t uknown[Q], uheads[Q], ureduced[Q], uprefix[Q], ufree[Q];
@@ -211,7 +211,7 @@ struct SegCtrl {
 
 template <class Op, int RW, int RS, int SS, int Q, int G, bool SEG>
 constexpr size_t seg_smem_bytes() {
-    return static_cast<size_t>(RS + SS) * TileShape<typename Op::T, RW>::kTile * sizeof(typename Op::T) +
+    return static_cast<size_t>(RS + SS) * 16384 +
            sizeof(SegCtrl<Op, RW, RS, SS, Q, G, SEG>);
 }
 
@@ -228,17 +228,21 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
     using T = typename Op::T;
     using S = typename Op::S;
     using C = typename Op::C;
-    using Shape = TileShape<T, RW>;
-    constexpr int TILE = Shape::kTile;
-    constexpr int ITEMS = Shape::kItems;
+    // A tile is 128 rows of 128 bytes (16 KB). Each role has RW warps:
+    // SPLIT = RW / 4 threads share a row (1 or 2), so a thread holds
+    // 128 / SPLIT bytes: ITEMS elements in CHUNKS 16-byte chunks.
+    constexpr int SPLIT = RW / 4;
+    constexpr int TILE = 16384 / static_cast<int>(sizeof(T));
+    constexpr int ITEMS = 128 / static_cast<int>(sizeof(T)) / SPLIT;
     constexpr int EPC = 16 / static_cast<int>(sizeof(T));
     constexpr int CHUNKS = ITEMS / EPC;
-    constexpr uint32_t NROLE = Shape::kRoleThreads;
+    constexpr uint32_t NROLE = RW * 32;
+    constexpr uint32_t ROWS = 128;  // rows per tile
     constexpr uint32_t LW = SegShape<Op, RW>::kLookbackWarps;
     constexpr uint32_t kWarpLookback = 4, kWarpReduce = 4 + LW, kWarpFinal = 4 + LW + RW;
     constexpr int kHeadWords = TILE / 32;
-    static_assert(CHUNKS == 8, "128 bytes per thread");
-    static_assert(NROLE == 128, "a tile is one box of 128 rows of 128 bytes");
+    static_assert((SPLIT == 1 || SPLIT == 2) && RW % 4 == 0, "4 or 8 warps per role");
+    static_assert(NROLE / SPLIT == ROWS, "a tile is one box of 128 rows of 128 bytes");
     static_assert(Q > LW, "every lookback warp needs its own queue entry");
     using Ctrl = SegCtrl<Op, RW, RS, SS, Q, G, SEG>;
 
@@ -297,43 +301,51 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
     // Bytes one TMA box brings for tile t (rows past the tensor are filled
     // with zeros and counted), or 0 when the tile has no full row.
     auto tma_bytes_of = [&](uint32_t t) -> uint32_t {
-        return (t < a.num_tiles && static_cast<uint64_t>(t) * NROLE < rows_full)
+        return (t < a.num_tiles && static_cast<uint64_t>(t) * ROWS < rows_full)
                    ? static_cast<uint32_t>(TILE * sizeof(T))
                    : 0u;
     };
-    // A thread's 128-byte row of tile t, in logical order.
+    // A thread's part of its 128-byte row of tile t (all of it, or one of
+    // two halves), in logical order. In the stage, chunk j of row r sits at
+    // j ^ (r & 7) (the 128-byte swizzle): 8 consecutive threads touch 8
+    // different 16-byte bank groups.
     auto load_row = [&](const T* stage, uint32_t t, uint32_t thr, T (&v)[ITEMS]) {
-        const uint64_t row = static_cast<uint64_t>(t) * NROLE + thr;
+        const uint32_t rit = thr / SPLIT, sub = thr % SPLIT;
+        const uint64_t row = static_cast<uint64_t>(t) * ROWS + rit;
         if (row < rows_full) {
-            const T* rp = stage + thr * ITEMS;
+            const T* rp = stage + rit * ROW;
 #pragma unroll
             for (int c = 0; c < CHUNKS; ++c) {
-                const Chunk<T> qv = *reinterpret_cast<const Chunk<T>*>(rp + (c ^ static_cast<int>(thr & 7u)) * EPC);
+                const int pos = (static_cast<int>(sub) * CHUNKS + c) ^ static_cast<int>(rit & 7u);
+                const Chunk<T> qv = *reinterpret_cast<const Chunk<T>*>(rp + pos * EPC);
 #pragma unroll
                 for (int e = 0; e < EPC; ++e) v[c * EPC + e] = qv.v[e];
             }
         } else {
-            const T* gp = static_cast<const T*>(a.in) + row * ROW;
+            const T* gp = static_cast<const T*>(a.in) + row * ROW + sub * ITEMS;
 #pragma unroll
-            for (int e = 0; e < ITEMS; ++e) v[e] = (row == rows_full && static_cast<uint32_t>(e) < tail) ? gp[e] : T(0);
+            for (int e = 0; e < ITEMS; ++e)
+                v[e] = (row == rows_full && sub * ITEMS + static_cast<uint32_t>(e) < tail) ? gp[e] : T(0);
         }
     };
     auto store_row = [&](T* stage, uint32_t t, uint32_t thr, const T (&v)[ITEMS]) {
-        const uint64_t row = static_cast<uint64_t>(t) * NROLE + thr;
+        const uint32_t rit = thr / SPLIT, sub = thr % SPLIT;
+        const uint64_t row = static_cast<uint64_t>(t) * ROWS + rit;
         if (row < rows_full) {
-            T* rp = stage + thr * ITEMS;
+            T* rp = stage + rit * ROW;
 #pragma unroll
             for (int c = 0; c < CHUNKS; ++c) {
                 Chunk<T> qv;
 #pragma unroll
                 for (int e = 0; e < EPC; ++e) qv.v[e] = v[c * EPC + e];
-                *reinterpret_cast<Chunk<T>*>(rp + (c ^ static_cast<int>(thr & 7u)) * EPC) = qv;
+                const int pos = (static_cast<int>(sub) * CHUNKS + c) ^ static_cast<int>(rit & 7u);
+                *reinterpret_cast<Chunk<T>*>(rp + pos * EPC) = qv;
             }
         } else if (row == rows_full) {
-            T* gp = static_cast<T*>(a.out) + row * ROW;
+            T* gp = static_cast<T*>(a.out) + row * ROW + sub * ITEMS;
 #pragma unroll
             for (int e = 0; e < ITEMS; ++e)
-                if (static_cast<uint32_t>(e) < tail) gp[e] = v[e];
+                if (sub * ITEMS + static_cast<uint32_t>(e) < tail) gp[e] = v[e];
         }
     };
     auto wait1 = [&](uint64_t* bar, uint32_t ph, uint64_t b) -> bool {
@@ -380,8 +392,8 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
 #pragma unroll
                     for (int k = 0; k < G; ++k) {
                         if (tma_bytes_of(u * G + k) == 0) continue;
-                        const uint64_t r0 = static_cast<uint64_t>(u * G + k) * NROLE;
-                        const uint64_t r1 = r0 + NROLE < rows_full ? r0 + NROLE : rows_full;
+                        const uint64_t r0 = static_cast<uint64_t>(u * G + k) * ROWS;
+                        const uint64_t r1 = r0 + ROWS < rows_full ? r0 + ROWS : rows_full;
                         ptx::bulk_prefetch_l2(static_cast<const T*>(a.in) + r0 * ROW, static_cast<uint32_t>((r1 - r0) * 128),
                                               pol);
                     }
@@ -414,7 +426,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                     const uint32_t bytes = tma_bytes_of(t);
                     ptx::mbar_arrive_expect_tx(&ctrl->rfull[s], bytes);
                     if (bytes)
-                        ptx::tma_load_2d(rbuf + static_cast<size_t>(s) * TILE, &tin, 0, static_cast<int32_t>(t * NROLE),
+                        ptx::tma_load_2d(rbuf + static_cast<size_t>(s) * TILE, &tin, 0, static_cast<int32_t>(t * ROWS),
                                          &ctrl->rfull[s], pol);
                 }
             }
@@ -465,7 +477,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                     const uint32_t bytes = tma_bytes_of(t);
                     ptx::mbar_arrive_expect_tx(&ctrl->sfull[s], bytes);
                     if (bytes)
-                        ptx::tma_load_2d(sbuf + static_cast<size_t>(s) * TILE, &tin, 0, static_cast<int32_t>(t * NROLE),
+                        ptx::tma_load_2d(sbuf + static_cast<size_t>(s) * TILE, &tin, 0, static_cast<int32_t>(t * ROWS),
                                          &ctrl->sfull[s], pol);
                 }
                 if (end) break;
@@ -487,7 +499,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                 if (t == kTileEnd) break;
                 // Rows past the tensor are clipped by the TMA unit.
                 if (tma_bytes_of(t))
-                    ptx::tma_store_2d(&tout, 0, static_cast<int32_t>(t * NROLE), sbuf + static_cast<size_t>(s) * TILE,
+                    ptx::tma_store_2d(&tout, 0, static_cast<int32_t>(t * ROWS), sbuf + static_cast<size_t>(s) * TILE,
                                       pol);
                 ptx::bulk_commit();
                 if (sn >= 1) {

@@ -12,7 +12,7 @@ namespace gps {
 // block (whose per-thread prefixes and head bitmaps grow with the state size
 // and the unit), taken as 4 reduce-pass + 9 scan-pass stages when 13 fit
 // (measured on GB300: 4 + 9 beats 5 + 8 by 3-8% on the batched workloads),
-// else 4 + 8, else 3 + 8. The unit (1 or 4 tiles) and the CTA count come from
+// else 4 + 8, 3 + 8, 3 + 7, 3 + 6. The unit (1 or 4 tiles) and the CTA count come from
 // the plan's launch configuration (GenericConfig).
 constexpr int kSegWarps = 4;
 constexpr int kSegQueue = 6;
@@ -20,20 +20,23 @@ constexpr size_t kMaxSmem = 232448;
 
 template <class Op, int G, bool SEG>
 struct SegStages {
-    static constexpr bool k13 = seg_smem_bytes<Op, kSegWarps, 4, 9, kSegQueue, G, SEG>() <= kMaxSmem;
-    static constexpr bool k12 = seg_smem_bytes<Op, kSegWarps, 4, 8, kSegQueue, G, SEG>() <= kMaxSmem;
+    static constexpr int RW = kSegWarps * Op::kSplit;  // warps per role
+    static constexpr bool k13 = seg_smem_bytes<Op, RW, 4, 9, kSegQueue, G, SEG>() <= kMaxSmem;
+    static constexpr bool k12 = seg_smem_bytes<Op, RW, 4, 8, kSegQueue, G, SEG>() <= kMaxSmem;
+    static constexpr bool k11 = seg_smem_bytes<Op, RW, 3, 8, kSegQueue, G, SEG>() <= kMaxSmem;
+    static constexpr bool k10 = seg_smem_bytes<Op, RW, 3, 7, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr int RS = (k13 || k12) ? 4 : 3;
-    static constexpr int SS = k13 ? 9 : 8;
-    static_assert(seg_smem_bytes<Op, kSegWarps, RS, SS, kSegQueue, G, SEG>() <= kMaxSmem, "227 KB per CTA");
+    static constexpr int SS = k13 ? 9 : (k12 || k11) ? 8 : k10 ? 7 : 6;
+    static_assert(seg_smem_bytes<Op, RW, RS, SS, kSegQueue, G, SEG>() <= kMaxSmem, "227 KB per CTA");
 };
 
 template <class Op, bool INCL, bool SEG, int UNIT>
 cudaError_t launch_seg_t(const ScanArgs& a, const SegArgs& sg, const GenericConfig& cfg, int num_sms,
                          cudaStream_t stream, LaunchInfo* info) {
     using St = SegStages<Op, UNIT, SEG>;
-    auto kern = scan_seg_kernel<Op, kSegWarps, St::RS, St::SS, kSegQueue, UNIT, INCL, SEG>;
-    constexpr size_t smem = seg_smem_bytes<Op, kSegWarps, St::RS, St::SS, kSegQueue, UNIT, SEG>();
-    constexpr int threads = SegShape<Op, kSegWarps>::kThreads;
+    auto kern = scan_seg_kernel<Op, St::RW, St::RS, St::SS, kSegQueue, UNIT, INCL, SEG>;
+    constexpr size_t smem = seg_smem_bytes<Op, St::RW, St::RS, St::SS, kSegQueue, UNIT, SEG>();
+    constexpr int threads = SegShape<Op, St::RW>::kThreads;
     RowMaps maps;
     cudaError_t err = encode_row_maps(a.in, a.out, a.n, static_cast<uint32_t>(sizeof(typename Op::T)), &maps);
     if (err != cudaSuccess) return err;
