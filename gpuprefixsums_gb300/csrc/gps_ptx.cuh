@@ -12,12 +12,6 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint32_t lane_id() {
-    uint32_t l;
-    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
-    return l;
-}
-
 __device__ __forceinline__ uint64_t global_timer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -143,10 +137,6 @@ __device__ __forceinline__ void tma_store_2d(const void* tmap, int32_t x, int32_
                      reinterpret_cast<uint64_t>(tmap)),
                  "r"(x), "r"(y), "r"(smem_addr(smem_src)), "l"(policy)
                  : "memory");
-}
-
-__device__ __forceinline__ void prefetch_tensormap(const void* tmap) {
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
 }
 
 // shared -> global with an L2 cache policy, tracked as a bulk async-group.
