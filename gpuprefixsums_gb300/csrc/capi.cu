@@ -48,6 +48,8 @@ struct gps_plan_s {
     // u32 kernel; on other plans they are hdr and area.
     gps::WsHeader* hdr16;
     void* desc16;
+    // Integer scans of at most this many elements run in one CTA (small.cu).
+    uint64_t small_max;
     // Autotuned launch configuration of the generic kernel per [segmented?]
     // [size class] (index into gps::kGenericCandidates; -1: not tuned).
     int8_t tuned[2][kSizeClasses];
@@ -142,6 +144,8 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
         a.desc = p->desc16;
         err = launch_generic(p->dtype, inclusive, a, nullptr, generic_config(p, false, n), p->num_sms, stream,
                              &p->last_launch);
+    } else if (n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
+        err = gps::launch_small(p->dtype, inclusive, a, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
         err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0 || p->stall.fallback_polls != 0, a, p->num_sms,
                                stream, &p->last_launch);
@@ -206,6 +210,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->capacity_tiles = tiles;
     p->wait_budget_ns = kDefaultBudgetNs;
     std::memset(p->tuned, -1, sizeof(p->tuned));
+    p->small_max = gps::small_scan_max_elems(dtype);
     cudaError_t err = cudaGetDevice(&p->device);
     if (err == cudaSuccess) err = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (err != cudaSuccess) {
@@ -607,7 +612,18 @@ gps_status gps_plan_geometry(gps_plan p, uint64_t n, uint32_t* tile_elems, uint3
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (tile_elems) *tile_elems = p->tile_elems;
     if (grid) *grid = static_cast<uint32_t>(p->last_launch.grid);
-    if (launches) *launches = n == 0 ? 0u : (p->algo == GPS_ALGO_CSDL ? 1u : 3u);
+    const bool small = !is_float(p->dtype) && n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0;
+    if (launches) *launches = n == 0 ? 0u : (small || p->algo == GPS_ALGO_CSDL ? 1u : 3u);
+    return GPS_OK;
+}
+
+gps_status gps_plan_set_small_max(gps_plan p, uint64_t max_n) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    const uint64_t cap = gps::small_scan_max_elems(p->dtype);
+    if (max_n > cap)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "the one-CTA scan takes at most %llu elements of this type",
+                    static_cast<unsigned long long>(cap));
+    p->small_max = max_n;
     return GPS_OK;
 }
 

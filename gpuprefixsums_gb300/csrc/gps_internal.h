@@ -155,6 +155,11 @@ uint32_t select_tile_elems(size_t elem_size);
 cudaError_t launch_select(size_t elem_size, const ScanArgs& a, const uint8_t* flags, int num_sms, cudaStream_t stream,
                           LaunchInfo* info);
 
+// Small integer scans in one CTA (small.cu): up to kSmallMaxBytes of input.
+constexpr size_t kSmallMaxBytes = 64 * 1024;
+uint64_t small_scan_max_elems(gps_dtype dtype);
+cudaError_t launch_small(gps_dtype dtype, bool inclusive, const ScanArgs& a, cudaStream_t stream, LaunchInfo* info);
+
 uint32_t csdl_tile_elems(gps_dtype dtype);
 // Sets the text gps_last_error() returns on this host thread.
 void record_error(const char* msg);

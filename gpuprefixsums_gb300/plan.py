@@ -173,6 +173,10 @@ class Plan:
         for this many lookback polls (0: off)."""
         check(lib.gps_plan_set_fallback(self._h, int(fallback_polls)), "gps_plan_set_fallback")
 
+    def set_small_max(self, max_n: int) -> None:
+        """Largest integer scan run in one CTA (0: always the multi-CTA kernels)."""
+        check(lib.gps_plan_set_small_max(self._h, int(max_n)), "gps_plan_set_small_max")
+
     def stats(self, stream=None) -> dict:
         s = _lib.LookbackStats()
         check(lib.gps_plan_stats(self._h, ctypes.c_void_p(_stream_handle(stream)), ctypes.byref(s)), "gps_plan_stats")

@@ -215,6 +215,13 @@ gps_status gps_plan_set_stall(gps_plan plan, uint32_t mode, uint32_t period, uin
  * which the CUDA part only shows in its EmulatedDeadlocking test. */
 gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
 
+/* Integer scans of at most max_n elements (default and maximum: 64 KB of
+ * input, 16384 u32 or 8192 u64) run in a single CTA instead of the
+ * persistent multi-CTA kernels, whose pipeline costs a fixed few
+ * microseconds; 0 sends every scan to the chained scan / reduce-then-scan
+ * kernels. Forced-stall and fallback modes always use the multi-CTA kernels. */
+gps_status gps_plan_set_small_max(gps_plan plan, uint64_t max_n);
+
 /* Lookback statistics gathered while forced-stall mode is on. Synchronizes
  * `stream`. */
 typedef struct gps_lookback_stats {

@@ -14,7 +14,7 @@
  *           busy) and Sklansky (each step broadcasts the last lane of the
  *           lower half of every 2d-lane group);
  *   block   raking over warp totals: each warp scans, the warp totals go
- *           through shared memory and every warp folds those before it;
+ *           through shared memory and every warp scans them again;
  *           THREADS a multiple of 32, at most 1024;
  *   thread  serial scan of ITEMS values in registers, and the "items per
  *           thread" tile scan that composes the three.
@@ -119,26 +119,32 @@ struct BlockScanStorage {
 };
 
 // Block scans: each warp scans its 32 values, the warp totals go through
-// shared memory, and every thread folds the totals of the warps before its
-// own (at most 31 broadcast reads) -- the raking step done redundantly per
-// warp, which costs one barrier instead of two. *block_total (if not null)
-// receives the block's total in every thread. Contain __syncthreads().
-template <int THREADS, typename T, typename Op = Plus>
-__device__ __forceinline__ T block_inclusive_scan(T x, BlockScanStorage<THREADS, T>& st, Op op = Op(),
-                                                  T* block_total = nullptr) {
+// shared memory, and every warp scans the (at most 32) warp totals itself --
+// one shared load per lane and one more warp scan instead of a second round
+// of barriers. *block_total (if not null) receives the block's total in
+// every thread. Contain __syncthreads().
+template <int THREADS, typename T, typename Op>
+__device__ __forceinline__ void block_prefix_of_warp(const BlockScanStorage<THREADS, T>& st, Op op, T& pre, T& tot) {
     constexpr int W = THREADS / 32;
     const uint32_t lane = lane_id();
     const uint32_t warp = threadIdx.x >> 5;
-    T inc = warp_inclusive_scan<WarpAlgo::KoggeStone>(x, op);
+    T t = lane < static_cast<uint32_t>(W) ? st.warp_totals[lane] : Op::template identity<T>();
+    t = warp_inclusive_scan<WarpAlgo::KoggeStone>(t, op);
+    const T before = __shfl_sync(0xFFFFFFFFu, t, warp == 0 ? 0u : warp - 1);
+    pre = warp == 0 ? Op::template identity<T>() : before;
+    tot = __shfl_sync(0xFFFFFFFFu, t, W - 1);
+}
+
+template <int THREADS, typename T, typename Op = Plus>
+__device__ __forceinline__ T block_inclusive_scan(T x, BlockScanStorage<THREADS, T>& st, Op op = Op(),
+                                                  T* block_total = nullptr) {
+    const uint32_t lane = lane_id();
+    const uint32_t warp = threadIdx.x >> 5;
+    const T inc = warp_inclusive_scan<WarpAlgo::KoggeStone>(x, op);
     if (lane == 31) st.warp_totals[warp] = inc;
     __syncthreads();
-    T pre = Op::template identity<T>(), tot = Op::template identity<T>();
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-        const T t = st.warp_totals[w];
-        if (static_cast<uint32_t>(w) < warp) pre = op(pre, t);
-        tot = op(tot, t);
-    }
+    T pre, tot;
+    block_prefix_of_warp(st, op, pre, tot);
     if (block_total) *block_total = tot;
     __syncthreads();  // the storage may be reused right after
     return op(pre, inc);
@@ -147,20 +153,14 @@ __device__ __forceinline__ T block_inclusive_scan(T x, BlockScanStorage<THREADS,
 template <int THREADS, typename T, typename Op = Plus>
 __device__ __forceinline__ T block_exclusive_scan(T x, BlockScanStorage<THREADS, T>& st, Op op = Op(),
                                                   T* block_total = nullptr) {
-    constexpr int W = THREADS / 32;
     const uint32_t lane = lane_id();
     const uint32_t warp = threadIdx.x >> 5;
     T wt;
     const T exc = warp_exclusive_scan<WarpAlgo::KoggeStone>(x, op, &wt);
     if (lane == 0) st.warp_totals[warp] = wt;
     __syncthreads();
-    T pre = Op::template identity<T>(), tot = Op::template identity<T>();
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-        const T t = st.warp_totals[w];
-        if (static_cast<uint32_t>(w) < warp) pre = op(pre, t);
-        tot = op(tot, t);
-    }
+    T pre, tot;
+    block_prefix_of_warp(st, op, pre, tot);
     if (block_total) *block_total = tot;
     __syncthreads();
     return op(pre, exc);

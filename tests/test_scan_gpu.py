@@ -52,11 +52,15 @@ def test_config1_2pow20_uniform_0_15(cuda, algo, inclusive):
 # -------------------------------------------- the reference's size sweep
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("inclusive", [False, True])
-def test_every_size_from_one_to_two_tiles_all_ones_in_place(cuda, algo, inclusive):
+@pytest.mark.parametrize("one_cta", [True, False])
+def test_every_size_from_one_to_two_tiles_all_ones_in_place(cuda, algo, inclusive, one_cta):
     # ChainedScanDecoupledLookbackDispatcher.cuh:48-59: every n in
     # [4096, 8192] on all-ones input, scanned in place; extended down to 1.
+    # Both through the one-CTA scan of small inputs and with it turned off.
     top = 2 * 4096 + 1
     with Plan(algo, "u32", max_n=top) as plan:
+        if not one_cta:
+            plan.set_small_max(0)
         buf = torch.empty(top, dtype=torch.int32, device="cuda")
         ar = torch.arange(top + 1, dtype=torch.int64, device="cuda")
         bad = []
@@ -73,7 +77,8 @@ def test_every_size_from_one_to_two_tiles_all_ones_in_place(cuda, algo, inclusiv
 @pytest.mark.parametrize("dtype", ["u32", "u64"])
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("inclusive", [False, True])
-def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive):
+@pytest.mark.parametrize("one_cta", [True, False])
+def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive, one_cta):
     # Full-range values (sums wrap), out of place, and words after n must
     # stay untouched (the reference writes up to align4(n)).
     rng = np.random.default_rng(99)
@@ -82,6 +87,8 @@ def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive):
                        rng.integers(1, 40 * t, size=12).tolist()))
     canary = 64
     with Plan(algo, dtype, max_n=max(sizes)) as plan:
+        if not one_cta:
+            plan.set_small_max(0)
         for n in sizes:
             x = rand(dtype, n, seed=n)
             d_in = to_dev(x)
@@ -96,7 +103,8 @@ def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive):
 
 @pytest.mark.parametrize("dtype", ["u32", "u64"])
 @pytest.mark.parametrize("algo", ALGOS)
-def test_unaligned_pointers_take_the_plain_path(cuda, dtype, algo):
+@pytest.mark.parametrize("one_cta", [True, False])
+def test_unaligned_pointers_take_the_plain_path(cuda, dtype, algo, one_cta):
     # Pointers aligned to the element but not to 16 bytes; in and out offset
     # differently.
     es = 4 if dtype == "u32" else 8
@@ -107,6 +115,8 @@ def test_unaligned_pointers_take_the_plain_path(cuda, dtype, algo):
         big_out = torch.zeros(n + 8, dtype=TORCH_VIEW[dtype][1], device="cuda")
         big_in[1:n + 1] = to_dev(x)
         with Plan(algo, dtype, max_n=n) as plan:
+            if not one_cta:
+                plan.set_small_max(0)
             plan.scan_ptr(big_in.data_ptr() + es, big_out.data_ptr() + 3 * es, n, inclusive=False)
             plan.check()
         got = to_host(big_out[3:n + 3], NP[dtype])
