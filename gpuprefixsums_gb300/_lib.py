@@ -23,6 +23,7 @@ DTYPE_U32 = 0
 DTYPE_U64 = 1
 DTYPE_F32 = 2
 DTYPE_F32_COMPENSATED = 3
+DTYPE_U32X4 = 4
 ALGO_CSDL = 0
 ALGO_RTS = 1
 EXCLUSIVE = 0

@@ -85,12 +85,16 @@ constexpr size_t kHeaderBytes = sizeof(gps::WsHeader);
 constexpr size_t kCarryBytes = 128;  // two carry slots, padded to a line
 constexpr uint64_t kDefaultBudgetNs = 1000000000ull;
 
-size_t desc_bytes(gps_dtype dtype) { return dtype == GPS_DTYPE_U32 ? 8 : 16; }
+size_t desc_bytes(gps_dtype dtype) { return dtype == GPS_DTYPE_U32 ? 8 : dtype == GPS_DTYPE_U32X4 ? 32 : 16; }
 
 bool valid_dtype(int d) {
-    return d == GPS_DTYPE_U32 || d == GPS_DTYPE_U64 || d == GPS_DTYPE_F32 || d == GPS_DTYPE_F32_COMPENSATED;
+    return d == GPS_DTYPE_U32 || d == GPS_DTYPE_U64 || d == GPS_DTYPE_F32 || d == GPS_DTYPE_F32_COMPENSATED ||
+           d == GPS_DTYPE_U32X4;
 }
 bool is_float(gps_dtype d) { return d == GPS_DTYPE_F32 || d == GPS_DTYPE_F32_COMPENSATED; }
+// Types whose every scan runs on the generic kernel (no L2, one-CTA or
+// reduce-then-scan kernel of their own).
+bool generic_only(gps_dtype d) { return is_float(d) || d == GPS_DTYPE_U32X4; }
 
 // Launch configuration of the generic kernel for a scan of n elements: the
 // autotuned one of the size class if there is one, else the default rule.
@@ -108,6 +112,7 @@ cudaError_t launch_generic(gps_dtype dtype, bool inclusive, const gps::ScanArgs&
         case GPS_DTYPE_U64: return gps::launch_seg_u64(inclusive, a, sg, cfg, num_sms, stream, info);
         case GPS_DTYPE_F32: return gps::launch_seg_f32(inclusive, a, sg, cfg, num_sms, stream, info);
         case GPS_DTYPE_F32_COMPENSATED: return gps::launch_seg_f32c(inclusive, a, sg, cfg, num_sms, stream, info);
+        case GPS_DTYPE_U32X4: return gps::launch_seg_u32x4(inclusive, a, sg, cfg, num_sms, stream, info);
     }
     return cudaErrorInvalidValue;
 }
@@ -139,7 +144,7 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     a.wait_budget_ns = p->wait_budget_ns;
     a.stall = p->stall;
     cudaError_t err;
-    if (is_float(p->dtype)) {
+    if (generic_only(p->dtype)) {
         a.hdr = p->hdr16;
         a.desc = p->desc16;
         err = launch_generic(p->dtype, inclusive, a, nullptr, generic_config(p, false, n), p->num_sms, stream,
@@ -159,7 +164,7 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
 }  // namespace
 
 namespace gps {
-size_t dtype_size(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 8 : 4; }
+size_t dtype_size(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 8 : dtype == GPS_DTYPE_U32X4 ? 16 : 4; }
 GenericConfig default_generic_config(uint64_t n, uint32_t tile_elems, int num_sms) {
     const uint64_t units4 = (n + 4ull * tile_elems - 1) / (4ull * tile_elems);
     return units4 >= 2ull * static_cast<uint64_t>(num_sms) ? GenericConfig{4, 1} : GenericConfig{1, 1};
@@ -193,8 +198,8 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     if (!valid_algo(algo)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown algorithm %d", static_cast<int>(algo));
     if (!valid_dtype(dtype)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown dtype %d", static_cast<int>(dtype));
     if (max_n == 0) return fail(GPS_ERR_INVALID_ARGUMENT, "max_n must be at least 1");
-    if (is_float(dtype) && algo != GPS_ALGO_CSDL)
-        return fail(GPS_ERR_UNSUPPORTED, "floating-point scans use the chained scan (GPS_ALGO_CSDL)");
+    if (generic_only(dtype) && algo != GPS_ALGO_CSDL)
+        return fail(GPS_ERR_UNSUPPORTED, "floating-point and struct scans use the chained scan (GPS_ALGO_CSDL)");
     const uint32_t tile = algo == GPS_ALGO_CSDL ? gps::csdl_tile_elems(dtype) : gps::rts_tile_elems(dtype);
     const uint64_t tiles = (max_n + tile - 1) / tile;
     if (tiles >= (1ull << 31))
@@ -304,8 +309,8 @@ gps_status gps_scan(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_ou
     const uint64_t bytes = n * es;
     if (i != o && i < o + bytes && o < i + bytes)
         return fail(GPS_ERR_INVALID_ARGUMENT, "input and output overlap without being identical");
-    if (is_float(p->dtype) && ((i | o) & 15u) != 0)
-        return fail(GPS_ERR_INVALID_ARGUMENT, "floating-point scans need 16-byte aligned buffers");
+    if (generic_only(p->dtype) && ((i | o) & 15u) != 0)
+        return fail(GPS_ERR_INVALID_ARGUMENT, "floating-point and struct scans need 16-byte aligned buffers");
     gps_status st = check_device(p);
     if (st != GPS_OK) return st;
     return launch_scan(p, kind == GPS_SCAN_INCLUSIVE, d_in, d_out, n, nullptr, nullptr,
@@ -322,7 +327,7 @@ gps_status prepare_generic(gps_plan_s* p, gps_scan_kind kind, const void* d_in, 
     if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
     if (p->algo != GPS_ALGO_CSDL)
         return fail(GPS_ERR_UNSUPPORTED, "batched scans run on chained-scan plans (GPS_ALGO_CSDL)");
-    if (d_offsets == nullptr && !is_float(p->dtype))
+    if (d_offsets == nullptr && !generic_only(p->dtype))
         return fail(GPS_ERR_UNSUPPORTED, "integer plans use the generic kernel for batched scans only");
     if (n == 0) return GPS_OK;
     if (d_offsets != nullptr && num_segments == 0)
@@ -444,6 +449,7 @@ gps_status gps_select_flagged(gps_plan p, const void* d_in, const uint8_t* d_fla
                               uint64_t* d_num_selected, gps_stream_t stream) {
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (p->algo != GPS_ALGO_CSDL) return fail(GPS_ERR_UNSUPPORTED, "select runs on chained-scan plans (GPS_ALGO_CSDL)");
+    if (p->dtype == GPS_DTYPE_U32X4) return fail(GPS_ERR_UNSUPPORTED, "select takes 4- or 8-byte elements");
     if (d_num_selected == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL count pointer");
     if ((reinterpret_cast<uintptr_t>(d_num_selected) & 7u) != 0)
         return fail(GPS_ERR_INVALID_ARGUMENT, "the count must be 8-byte aligned");
@@ -488,7 +494,7 @@ gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void*
     if (!valid_kind(kind)) return fail(GPS_ERR_INVALID_ARGUMENT, "unknown scan kind %d", static_cast<int>(kind));
     if (n == 0) return GPS_OK;
     if (h_in == nullptr || h_out == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "NULL data pointer");
-    if (is_float(p->dtype)) return fail(GPS_ERR_UNSUPPORTED, "host-array scans are integer only");
+    if (generic_only(p->dtype)) return fail(GPS_ERR_UNSUPPORTED, "host-array scans take u32 and u64 plans");
     gps_status st = check_device(p);
     if (st != GPS_OK) return st;
     const size_t es = gps::dtype_size(p->dtype);
@@ -612,7 +618,7 @@ gps_status gps_plan_geometry(gps_plan p, uint64_t n, uint32_t* tile_elems, uint3
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (tile_elems) *tile_elems = p->tile_elems;
     if (grid) *grid = static_cast<uint32_t>(p->last_launch.grid);
-    const bool small = !is_float(p->dtype) && n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0;
+    const bool small = !generic_only(p->dtype) && n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0;
     if (launches) *launches = n == 0 ? 0u : (small || p->algo == GPS_ALGO_CSDL ? 1u : 3u);
     return GPS_OK;
 }

@@ -89,6 +89,8 @@ cudaError_t dispatch_csdl(bool inclusive, bool stall, const ScanArgs& a, int num
 }  // namespace
 
 uint32_t csdl_tile_elems(gps_dtype dtype) {
+    // Struct elements (16 bytes) run on the generic kernel's 16 KB tiles.
+    if (dtype == GPS_DTYPE_U32X4) return 16384 / 16;
     return dtype == GPS_DTYPE_U64 ? TileShape<uint64_t, kCsdlWarps>::kTile : TileShape<uint32_t, kCsdlWarps>::kTile;
 }
 

@@ -148,6 +148,8 @@ cudaError_t launch_seg_f32(bool inclusive, const ScanArgs& a, const SegArgs* sg,
                            cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
                             int num_sms, cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_u32x4(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                             int num_sms, cudaStream_t stream, LaunchInfo* info);
 
 // Stream compaction by flag bytes (select.cu): elements per tile for an
 // element size, and the launch. a.carry_out receives the count (uint64).

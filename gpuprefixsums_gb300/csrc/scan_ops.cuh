@@ -57,6 +57,9 @@ struct OpInt {
     __device__ static C chain_add(C a, C b) { return a + b; }
     __device__ static uint64_t chain_bits(C c) { return static_cast<uint64_t>(c); }
     __device__ static C chain_from_bits(uint64_t b) { return static_cast<C>(b); }
+    static constexpr int kDescWords = 1;
+    __device__ static uint64_t chain_word(C c, int) { return chain_bits(c); }
+    __device__ static C chain_from_words(const uint64_t* w) { return chain_from_bits(w[0]); }
     __device__ static S shfl(S s, uint32_t src) { return shfl_any(s, src); }
     __device__ static S shfl_up(S s, uint32_t d) { return shfl_up_any(s, d); }
     __device__ static C chain_shfl_xor(C c, uint32_t m) { return __shfl_xor_sync(0xFFFFFFFFu, c, m); }
@@ -86,6 +89,9 @@ struct OpF32 {
     __device__ static C chain_add(C a, C b) { return a + b; }
     __device__ static uint64_t chain_bits(C c) { return __float_as_uint(c); }
     __device__ static C chain_from_bits(uint64_t b) { return __uint_as_float(static_cast<uint32_t>(b)); }
+    static constexpr int kDescWords = 1;
+    __device__ static uint64_t chain_word(C c, int) { return chain_bits(c); }
+    __device__ static C chain_from_words(const uint64_t* w) { return chain_from_bits(w[0]); }
     __device__ static S shfl(S s, uint32_t src) { return shfl_any(s, src); }
     __device__ static S shfl_up(S s, uint32_t d) { return shfl_up_any(s, d); }
     __device__ static C chain_shfl_xor(C c, uint32_t m) { return __shfl_xor_sync(0xFFFFFFFFu, c, m); }
@@ -156,6 +162,9 @@ struct OpF32C {
     __device__ static C chain_add(C a, C b) { return a + b; }
     __device__ static uint64_t chain_bits(C c) { return static_cast<uint64_t>(__double_as_longlong(c)); }
     __device__ static C chain_from_bits(uint64_t b) { return __longlong_as_double(static_cast<long long>(b)); }
+    static constexpr int kDescWords = 1;
+    __device__ static uint64_t chain_word(C c, int) { return chain_bits(c); }
+    __device__ static C chain_from_words(const uint64_t* w) { return chain_from_bits(w[0]); }
     __device__ static S shfl(S s, uint32_t src) {
         return F2{__shfl_sync(0xFFFFFFFFu, s.hi, src), __shfl_sync(0xFFFFFFFFu, s.lo, src)};
     }
@@ -163,6 +172,51 @@ struct OpF32C {
         return F2{__shfl_up_sync(0xFFFFFFFFu, s.hi, d), __shfl_up_sync(0xFFFFFFFFu, s.lo, d)};
     }
     __device__ static C chain_shfl_xor(C c, uint32_t m) { return __shfl_xor_sync(0xFFFFFFFFu, c, m); }
+};
+
+// ------------------------------------------------ four u32 members (struct)
+// Elements of four independent u32 members, each scanned on its own (wrapping
+// mod 2^32): a struct scan of vec4<u32>, as the reference's WebGPU struct
+// variant scans four members with per-member descriptors
+// (GPUPrefixSumsWebGPUapis/SharedShaders/csdldf_struct.wgsl:19,144-300). The
+// 128-bit chain value takes two descriptor words.
+struct OpU32x4 {
+    using T = uint4;
+    using S = uint4;
+    using C = uint4;
+    static constexpr bool kL2Prefetch = true;
+    static constexpr int kSplit = 1;
+    static constexpr int kDescWords = 2;
+    __device__ static S zero() { return make_uint4(0u, 0u, 0u, 0u); }
+    __device__ static S lift(T x) { return x; }
+    __device__ static S add(S a, S b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+    __device__ static S acc(S a, T x) { return add(a, x); }
+    __device__ static S combine(S a, S b) { return add(a, b); }
+    __device__ static S norm(S a) { return a; }
+    __device__ static T out(S s) { return s; }
+    __device__ static C to_chain(S s) { return s; }
+    __device__ static S from_chain(C c) { return c; }
+    __device__ static C chain_zero() { return zero(); }
+    __device__ static C chain_add(C a, C b) { return add(a, b); }
+    __device__ static uint64_t chain_word(C c, int w) {
+        return w == 0 ? (static_cast<uint64_t>(c.y) << 32) | c.x : (static_cast<uint64_t>(c.w) << 32) | c.z;
+    }
+    __device__ static C chain_from_words(const uint64_t* w) {
+        return make_uint4(static_cast<uint32_t>(w[0]), static_cast<uint32_t>(w[0] >> 32), static_cast<uint32_t>(w[1]),
+                          static_cast<uint32_t>(w[1] >> 32));
+    }
+    __device__ static S shfl(S s, uint32_t src) {
+        return make_uint4(__shfl_sync(0xFFFFFFFFu, s.x, src), __shfl_sync(0xFFFFFFFFu, s.y, src),
+                          __shfl_sync(0xFFFFFFFFu, s.z, src), __shfl_sync(0xFFFFFFFFu, s.w, src));
+    }
+    __device__ static S shfl_up(S s, uint32_t d) {
+        return make_uint4(__shfl_up_sync(0xFFFFFFFFu, s.x, d), __shfl_up_sync(0xFFFFFFFFu, s.y, d),
+                          __shfl_up_sync(0xFFFFFFFFu, s.z, d), __shfl_up_sync(0xFFFFFFFFu, s.w, d));
+    }
+    __device__ static C chain_shfl_xor(C c, uint32_t m) {
+        return make_uint4(__shfl_xor_sync(0xFFFFFFFFu, c.x, m), __shfl_xor_sync(0xFFFFFFFFu, c.y, m),
+                          __shfl_xor_sync(0xFFFFFFFFu, c.z, m), __shfl_xor_sync(0xFFFFFFFFu, c.w, m));
+    }
 };
 
 }  // namespace gps

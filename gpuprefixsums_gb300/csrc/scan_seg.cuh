@@ -94,17 +94,53 @@ __device__ __forceinline__ void thread_outputs(typename Op::T (&v)[ITEMS], typen
     }
 }
 
-// Lookback over 128-bit generic descriptors (see lookback() in
+// A unit's descriptor is Op::kDescWords 128-bit words, each carrying one
+// 64-bit word of the chain value with the status, head flag and epoch: a
+// reader takes the value only when every word has the launch's epoch and
+// the same status (a word that is one publication behind reads as not
+// ready).
+template <class Op>
+__device__ __forceinline__ void desc_store(ptx::u64x2* desc, uint64_t u, uint32_t status, bool flag, uint32_t epoch,
+                                           typename Op::C c) {
+#pragma unroll
+    for (int w = 0; w < Op::kDescWords; ++w)
+        ptx::st_relaxed_b128(desc + u * Op::kDescWords + w, seg_pack(status, flag, epoch, Op::chain_word(c, w)));
+}
+
+template <class Op>
+__device__ __forceinline__ uint32_t desc_load(const ptx::u64x2* desc, uint64_t u, uint32_t epoch, bool& flag,
+                                              typename Op::C& c) {
+    uint64_t words[Op::kDescWords];
+    uint32_t st = kNotReady;
+#pragma unroll
+    for (int w = 0; w < Op::kDescWords; ++w) {
+        const ptx::u64x2 x = ptx::ld_relaxed_b128(desc + u * Op::kDescWords + w);
+        const uint32_t s = (static_cast<uint32_t>(x.hi) & kEpochMask) == (epoch & kEpochMask)
+                               ? static_cast<uint32_t>(x.hi >> 62)
+                               : kNotReady;
+        if (w == 0) {
+            st = s;
+            flag = (x.hi & kHeadFlagBit) != 0;
+        } else if (s != st) {
+            st = kNotReady;
+        }
+        words[w] = x.lo;
+    }
+    if (st != kNotReady) c = Op::chain_from_words(words);
+    return st;
+}
+
+// Lookback over the generic descriptors (see lookback() in
 // scan_pipeline.cuh for the scheme): terminators are inclusive prefixes and
 // units holding a segment head. Returns the chain value before unit u.
 template <class Op>
 __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane, int64_t bound,
                                        typename Op::C bound_val) {
     using C = typename Op::C;
-    constexpr int K = 8;  // 16-byte descriptors per lane per window
+    constexpr int K = 8 / Op::kDescWords;  // descriptors per lane per window
     constexpr int WIN = 32 * K;
     constexpr uint32_t kNone = 0xFFFFFFFFu;
-    ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
+    const ptx::u64x2* desc = static_cast<const ptx::u64x2*>(a.desc);
     C prefix = Op::chain_zero();
     int64_t top = static_cast<int64_t>(u) - 1;
     uint32_t polls = 0;
@@ -131,14 +167,14 @@ __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t e
 #pragma unroll
             for (int j = 0; j < K; ++j) {
                 if ((pending >> j) & 1u) {
-                    const ptx::u64x2 w = ptx::ld_relaxed_b128(desc + slot_idx(j));
-                    const bool ok = (static_cast<uint32_t>(w.hi) & kEpochMask) == (epoch & kEpochMask);
-                    const uint32_t st = ok ? static_cast<uint32_t>(w.hi >> 62) : kNotReady;
+                    bool hf = false;
+                    C cv;
+                    const uint32_t st = desc_load<Op>(desc, static_cast<uint64_t>(slot_idx(j)), epoch, hf, cv);
                     if (st != kNotReady) {
                         valid |= 1u << j;
                         pending &= ~(1u << j);
-                        val[j] = Op::chain_from_bits(w.lo);
-                        if (st == kInclusive || (w.hi & kHeadFlagBit)) term |= 1u << j;
+                        val[j] = cv;
+                        if (st == kInclusive || hf) term |= 1u << j;
                     }
                 }
             }
@@ -325,7 +361,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             const T* gp = static_cast<const T*>(a.in) + row * ROW + sub * ITEMS;
 #pragma unroll
             for (int e = 0; e < ITEMS; ++e)
-                v[e] = (row == rows_full && sub * ITEMS + static_cast<uint32_t>(e) < tail) ? gp[e] : T(0);
+                v[e] = (row == rows_full && sub * ITEMS + static_cast<uint32_t>(e) < tail) ? gp[e] : T{};
         }
     };
     auto store_row = [&](T* stage, uint32_t t, uint32_t thr, const T (&v)[ITEMS]) {
@@ -517,7 +553,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                 uint32_t e = epoch + 1;
                 if ((e & kEpochMask) == 0) {
                     ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
-                    for (unsigned long long q = 0; q < a.hdr->capacity_tiles; ++q)
+                    for (unsigned long long q = 0; q < a.hdr->capacity_tiles * Op::kDescWords; ++q)
                         ptx::st_relaxed_b128(desc + q, ptx::u64x2{0, 0});
                     e += 1;
                 }
@@ -650,7 +686,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             const bool flag = ctrl->uflag[q] != 0;
             const C incl = flag ? agg : Op::chain_add(pre, agg);
             if (lane == 0) {
-                if (u != 0) ptx::st_relaxed_b128(desc + u, seg_pack(kInclusive, flag, epoch, Op::chain_bits(incl)));
+                if (u != 0) desc_store<Op>(desc, u, kInclusive, flag, epoch, incl);
                 ctrl->upre[q] = pre;
                 ptx::mbar_arrive(&ctrl->uprefix[q]);
             }
@@ -740,8 +776,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                 if (r == 0) {
                     const uint32_t u = t / G;
                     const C chain = Op::to_chain(unit_agg);
-                    ptx::st_relaxed_b128(desc + u, seg_pack(u == 0 ? kInclusive : kAggregate, unit_flag, epoch,
-                                                            Op::chain_bits(chain)));
+                    desc_store<Op>(desc, u, u == 0 ? kInclusive : kAggregate, unit_flag, epoch, chain);
                     ctrl->uagg[q] = chain;
                     ctrl->uflag[q] = unit_flag;
                     ptx::mbar_arrive(&ctrl->ureduced[q]);

@@ -31,6 +31,11 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 cudaError_t encode_one(CUtensorMap* map, const void* base, uint64_t n, uint32_t elem_size) {
     auto fn = encode_fn();
     if (fn == nullptr) return cudaErrorNotSupported;
+    // 16-byte struct elements travel as four 32-bit words each.
+    if (elem_size == 16) {
+        n *= 4;
+        elem_size = 4;
+    }
     const uint64_t row_elems = 128 / elem_size;
     // Row coordinates are 32-bit signed in the copy instructions.
     if (n / row_elems > 0x7FFFFF00ull) return cudaErrorInvalidValue;

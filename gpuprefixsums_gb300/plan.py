@@ -14,8 +14,9 @@ from . import _lib
 from ._lib import check, lib
 
 _ALGOS = {"csdl": _lib.ALGO_CSDL, "rts": _lib.ALGO_RTS}
-_DTYPES = {"u32": (_lib.DTYPE_U32, 4), "u64": (_lib.DTYPE_U64, 8), "f32": (_lib.DTYPE_F32, 4),
-           "f32c": (_lib.DTYPE_F32_COMPENSATED, 4)}
+# name -> (gps_dtype, bytes per tensor element, tensor elements per scanned element)
+_DTYPES = {"u32": (_lib.DTYPE_U32, 4, 1), "u64": (_lib.DTYPE_U64, 8, 1), "f32": (_lib.DTYPE_F32, 4, 1),
+           "f32c": (_lib.DTYPE_F32_COMPENSATED, 4, 1), "u32x4": (_lib.DTYPE_U32X4, 4, 4)}
 
 
 def _stream_handle(stream) -> int:
@@ -35,6 +36,9 @@ class Plan:
             raise ValueError(f"dtype must be one of {sorted(_DTYPES)}")
         self.algo, self.dtype, self.max_n = algo, dtype, int(max_n)
         self.elem_size = _DTYPES[dtype][1]
+        # u32x4: a struct of four u32 members; tensors hold n structs as 4n
+        # 32-bit words (shape (n, 4)), and sizes count structs.
+        self.members = _DTYPES[dtype][2]
         h = ctypes.c_void_p()
         check(lib.gps_plan_create(ctypes.byref(h), _ALGOS[algo], _DTYPES[dtype][0], self.max_n), "gps_plan_create")
         self._h = h
@@ -68,6 +72,12 @@ class Plan:
         check(lib.gps_scan(self._h, kind, ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr), int(n),
                            ctypes.c_void_p(_stream_handle(stream))), "gps_scan")
 
+    def length(self, x) -> int:
+        """Number of scanned elements in tensor x (structs for u32x4)."""
+        if x.numel() % self.members:
+            raise ValueError(f"a {self.dtype} tensor holds a multiple of {self.members} words")
+        return x.numel() // self.members
+
     def scan(self, x, out=None, inclusive: bool = False, n: int | None = None, stream=None):
         """Scan the first n elements of CUDA tensor x into out (allocated if None;
         out may be x for an in-place scan). Bits are taken as unsigned."""
@@ -80,8 +90,8 @@ class Plan:
             out = torch.empty_like(x)
         if out.element_size() != self.elem_size or not out.is_contiguous():
             raise ValueError("out must be contiguous with the plan's element size")
-        count = x.numel() if n is None else int(n)
-        if count > x.numel() or count > out.numel():
+        count = self.length(x) if n is None else int(n)
+        if count > self.length(x) or count > self.length(out):
             raise ValueError("n exceeds the tensor length")
         self.scan_ptr(x.data_ptr(), out.data_ptr(), count, inclusive, stream)
         return out
@@ -89,7 +99,8 @@ class Plan:
     def scan_segmented(self, x, offsets, out=None, inclusive: bool = False, stream=None):
         """Batched scan: independent scans of the segments [offsets[s],
         offsets[s+1]) of CUDA tensor x (offsets: int32/uint32 CUDA tensor of
-        num_segments + 1 entries, offsets[0] == 0, offsets[-1] == x.numel())."""
+        num_segments + 1 entries, offsets[0] == 0, offsets[-1] == the number of
+        elements, structs for u32x4)."""
         if x.element_size() != self.elem_size or not (x.is_cuda and x.is_contiguous()):
             raise ValueError("x must be a contiguous CUDA tensor with the plan's element size")
         if offsets.element_size() != 4 or not (offsets.is_cuda and offsets.is_contiguous()):
@@ -99,7 +110,7 @@ class Plan:
             out = torch.empty_like(x)
         kind = _lib.INCLUSIVE if inclusive else _lib.EXCLUSIVE
         check(lib.gps_scan_segmented(self._h, kind, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-                                     x.numel(), ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1,
+                                     self.length(x), ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1,
                                      ctypes.c_void_p(_stream_handle(stream))), "gps_scan_segmented")
         return out
 
@@ -135,7 +146,7 @@ class Plan:
         off_ptr = ctypes.c_void_p(offsets.data_ptr()) if offsets is not None else ctypes.c_void_p()
         nseg = offsets.numel() - 1 if offsets is not None else 0
         check(lib.gps_plan_autotune(self._h, kind, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-                                    x.numel(), off_ptr, nseg, ctypes.c_void_p(_stream_handle(stream)),
+                                    self.length(x), off_ptr, nseg, ctypes.c_void_p(_stream_handle(stream)),
                                     ctypes.byref(unit), ctypes.byref(div)), "gps_plan_autotune")
         return {"unit_tiles": unit.value, "ctas_div": div.value}
 

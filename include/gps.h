@@ -60,7 +60,13 @@ typedef enum gps_dtype {
     /* float in and out; each partial sum carries a TwoSum error term through
      * the thread, warp and block scans, and the value passed between lookback
      * units is FP64 (GPS_ALGO_CSDL only) */
-    GPS_DTYPE_F32_COMPENSATED = 3
+    GPS_DTYPE_F32_COMPENSATED = 3,
+    /* struct of four uint32_t members (16 bytes, e.g. uint4), each member
+     * scanned on its own and wrapping mod 2^32 -- the reference's vec4 struct
+     * scan (GPUPrefixSumsWebGPUapis/SharedShaders/csdldf_struct.wgsl:19,
+     * 144-300); n counts structs; 16-byte aligned buffers (GPS_ALGO_CSDL
+     * only) */
+    GPS_DTYPE_U32X4 = 4
 } gps_dtype;
 
 typedef enum gps_algo {

@@ -133,3 +133,25 @@ def select(x: np.ndarray, flags: np.ndarray) -> np.ndarray:
     out = np.empty_like(x)
     count = lib().oracle_select(_ptr(x), _ptr(flags), _ptr(out), x.size, x.itemsize)
     return out[:count]
+
+
+def scan_members(x: np.ndarray, offsets: np.ndarray | None = None, inclusive: bool = False) -> np.ndarray:
+    """Struct scan: x has shape (n, m), uint32; every member (column) is
+    scanned on its own, wrapping mod 2^32, within each segment when offsets
+    is given. The reference scans vec4<u32> structs this way, one lookback
+    descriptor per member (GPUPrefixSumsWebGPUapis/SharedShaders/
+    csdldf_struct.wgsl:144-300, inclusive)."""
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    if x.ndim != 2:
+        raise ValueError("x must have shape (n, members)")
+    cols = [np.ascontiguousarray(x[:, k]) for k in range(x.shape[1])]
+    if offsets is None:
+        return np.stack([scan(c, inclusive) for c in cols], axis=1)
+    return np.stack([segscan(c, offsets, inclusive) for c in cols], axis=1)
+
+
+def expected_struct_ones(words: int) -> np.ndarray:
+    """The reference's known answer for the struct scan of all-ones input:
+    word i of the inclusive result is i // 4 + 1
+    (GPUPrefixSumsWebGPUapis/SharedShaders/validate.wgsl:51-59)."""
+    return (np.arange(words, dtype=np.uint64) // 4 + 1).astype(np.uint32)

@@ -147,3 +147,27 @@ def test_select_matches_boolean_indexing():
         flags = (rng.random(x.size) < 0.3).astype(np.uint8) * rng.integers(1, 256, size=x.size).astype(np.uint8)
         assert np.array_equal(oracle.select(x, flags), x[flags != 0])
     assert oracle.select(np.zeros(0, np.uint32), np.zeros(0, np.uint8)).size == 0
+
+
+@pytest.mark.parametrize("inclusive", [False, True])
+def test_struct_scan_scans_each_member(inclusive):
+    rng = np.random.default_rng(21)
+    x = rng.integers(0, 1 << 32, size=(777, 4), dtype=np.uint64).astype(np.uint32)
+    got = oracle.scan_members(x, inclusive=inclusive)
+    for k in range(4):
+        assert got[:, k].tolist() == py_scan(x[:, k].tolist(), inclusive, 1 << 32)
+    lens = rng.integers(0, 60, size=25)
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    y = x[: int(offs[-1])]
+    seg = oracle.scan_members(y, offs, inclusive)
+    for s in range(len(lens)):
+        b, e = int(offs[s]), int(offs[s + 1])
+        for k in range(4):
+            assert seg[b:e, k].tolist() == py_scan(y[b:e, k].tolist(), inclusive, 1 << 32)
+
+
+@pytest.mark.parametrize("structs", [1, 1024, 4096 + 3, 1 << 16])
+def test_struct_scan_known_answer_of_all_ones(structs):
+    # Inclusive scan of all-ones structs: word i of the result is i // 4 + 1.
+    got = oracle.scan_members(np.ones((structs, 4), np.uint32), inclusive=True)
+    assert np.array_equal(got.reshape(-1), oracle.expected_struct_ones(4 * structs))
