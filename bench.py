@@ -67,10 +67,10 @@ def parse_args():
     p.add_argument("--no-compare", action="store_true",
                    help="only the timed scans (for profiling): no copy/CUB/RTS/e2e/CPU legs")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, fp32 and mixed workloads")
-    p.add_argument("--profile-case", choices=["batched", "f32c", "select"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "f32c", "select", "struct"], default=None,
                    help="launch one small case three times and exit (ncu captures): 1024 of the batched "
-                        "workload's segments, 2^26 compensated-f32 elements, or a select of 2^26 u32 by "
-                        "Bernoulli(0.3) flags")
+                        "workload's segments, 2^26 compensated-f32 elements, a select of 2^26 u32 by "
+                        "Bernoulli(0.3) flags, or an inclusive scan of 2^24 structs of four u32")
     p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
@@ -345,6 +345,50 @@ def run_select(stream, copy_gbs, reps=20):
             cub_call()
         cub_ms = time_loop(cub_call, reps, stream)
         res["cub_select_ms"] = round(cub_ms, 4)
+        res["ours_vs_cub"] = round(cub_ms / ms, 3)
+    except Exception as e:  # comparison only
+        res["cub_error"] = str(e)[:200]
+    return res
+
+
+def run_struct(stream, copy_gbs, reps=20):
+    """Struct scan: inclusive scan of 2^26 structs of four u32 members (1 GiB
+    in, 1 GiB out), each member on its own; against CUB's DeviceScan with a
+    member-wise sum on the same data."""
+    import torch
+
+    from gpuprefixsums_gb300 import Plan
+    from gpuprefixsums_gb300 import build as gbuild
+    n = 1 << 26
+    gen = torch.Generator(device="cuda").manual_seed(404)
+    x = torch.randint(-2 ** 31, 2 ** 31 - 1, (n, 4), dtype=torch.int32, device="cuda", generator=gen)
+    out = torch.empty_like(x)
+    res = {"workload": "inclusive struct scan of 2^26 x (4 x u32) = 1 GiB (member-wise, one launch)"}
+    with Plan("csdl", "u32x4", max_n=n) as plan:
+        step = lambda: plan.scan(x, out, inclusive=True, stream=stream)  # noqa: E731
+        for _ in range(3):
+            step()
+        ms = time_loop(step, reps, stream)
+        plan.check(stream)
+    if not (torch.equal(out[1:] - out[:-1], x[1:]) and torch.equal(out[0], x[0])):
+        raise SystemExit("bench: struct scan result is wrong; refusing to report a number")
+    gbs = n * 32 / (ms * 1e-3) / 1e9
+    res.update({"ms": round(ms, 4), "gbs": round(gbs, 2), "structs_per_s": round(n / (ms * 1e-3), 1),
+                "pct_of_copy": round(100.0 * gbs / copy_gbs, 2) if copy_gbs else None})
+    try:
+        cub = ctypes.CDLL(gbuild.build_cub_compare())
+        cub.gps_cub_scan_u32x4.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]
+        tb = ctypes.c_size_t(0)
+        cub.gps_cub_scan_u32x4(x.data_ptr(), out.data_ptr(), n, None, ctypes.byref(tb), None)
+        temp = torch.empty(max(1, tb.value), dtype=torch.uint8, device="cuda")
+        sp = ctypes.c_void_p(stream.cuda_stream)
+        cub_call = lambda: cub.gps_cub_scan_u32x4(x.data_ptr(), out.data_ptr(), n, temp.data_ptr(),  # noqa: E731
+                                                  ctypes.byref(tb), sp)
+        for _ in range(3):
+            cub_call()
+        cub_ms = time_loop(cub_call, reps, stream)
+        res["cub_ms"] = round(cub_ms, 4)
         res["ours_vs_cub"] = round(cub_ms / ms, 3)
     except Exception as e:  # comparison only
         res["cub_error"] = str(e)[:200]
@@ -642,6 +686,7 @@ def run_ours(args, world, rank, local):
             extras["fp32"] = run_fp32(stream)
             extras["mixed"] = run_mixed(stream, compare.get("d2d_copy_gbs"))
             extras["select"] = run_select(stream, compare.get("d2d_copy_gbs"))
+            extras["struct"] = run_struct(stream, compare.get("d2d_copy_gbs"))
 
         if rank == 0 and world == 1:
             import oracle
@@ -714,6 +759,14 @@ def run_profile_case(args):
                 out, cnt = plan.select(x, fl)
             plan.check()
         out = out[:int(cnt.item())]
+    elif args.profile_case == "struct":
+        n = 1 << 24  # 256 MiB of structs
+        x = torch.randint(-2 ** 31, 2 ** 31 - 1, (n, 4), dtype=torch.int32, device="cuda")
+        with Plan("csdl", "u32x4", max_n=n) as plan:
+            for _ in range(3):
+                out = plan.scan(x, inclusive=True)
+            plan.check()
+        out = out[:, 0]
     else:
         n = 1 << 26
         x = torch.randn(n, device="cuda")

@@ -35,6 +35,21 @@ int gps_cub_scan_u64(int inclusive, const void* in, void* out, uint64_t n, void*
     return static_cast<int>(err);
 }
 
+// Member-wise sum of four u32 (a struct of four independent counters).
+struct U32x4Plus {
+    __host__ __device__ uint4 operator()(const uint4& a, const uint4& b) const {
+        return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+    }
+};
+
+// Query (temp == nullptr) or run CUB's inclusive scan of n uint4 structs with
+// the member-wise sum.
+int gps_cub_scan_u32x4(const void* in, void* out, uint64_t n, void* temp, size_t* temp_bytes, cudaStream_t stream) {
+    return static_cast<int>(cub::DeviceScan::InclusiveScan(temp, *temp_bytes, static_cast<const uint4*>(in),
+                                                           static_cast<uint4*>(out), U32x4Plus(),
+                                                           static_cast<int64_t>(n), stream));
+}
+
 // Query (temp == nullptr) or run CUB's DeviceSelect::Flagged of n u32 with
 // one flag byte each; the count goes to *num_selected (device, int64).
 int gps_cub_select_u32(const void* in, const void* flags, void* out, void* num_selected, uint64_t n, void* temp,
