@@ -225,7 +225,7 @@ struct SegCtrl {
     static constexpr int kHeadWords = 16384 / static_cast<int>(sizeof(typename Op::T)) / 32;
     uint64_t rfull[RS], rfree[RS];
     uint64_t sfull[SS], sdone[SS], sfree[SS];
-    uint64_t uknown[Q], uheads[Q], ureduced[Q], uprefix[Q], ufree[Q];
+    uint64_t uknown[Q], uheads[Q], uentries[Q], ureduced[Q], uprefix[Q], ufree[Q];
     uint32_t r_tile[RS];
     uint32_t s_tile[SS];
     uint32_t unit_of[Q];
@@ -233,13 +233,18 @@ struct SegCtrl {
     uint32_t uflag[Q];  // unit holds a segment head
     C uagg[Q];
     C upre[Q];
-    S r_wtot[2][RW];
-    uint32_t r_wflag[2][RW];
-    // From the reduce pass to the scan pass: the state before each thread's
-    // 128 bytes within its unit, and (bit = lane) whether a segment head lies
-    // between the unit's start and that thread.
-    S tpre[Q][G][RW * 32];
-    uint32_t tflag[Q][G][RW];
+    // Per unit, one entry per reduce thread and tile (E = G * RW * 32, in
+    // unit order): the reduce warps leave each thread's aggregate there, the
+    // aggregator warp replaces it by the state before that thread within the
+    // unit, which the scan pass reads. Entry j sits at j + j / (G * RW), so
+    // that the aggregator's lanes, which take G * RW consecutive entries
+    // each, and the threads of a warp, which take consecutive ones, both
+    // meet distinct banks.
+    static constexpr int kEntries = G * RW * 32;
+    S tpre[Q][kEntries + 32];
+    // Segmented scans: per entry, first "the thread's items hold a head",
+    // then "a head lies between the unit's start and the thread".
+    uint8_t tflag[SEG ? Q : 1][SEG ? kEntries : 1];
     // Segmented scans only (one unused entry otherwise):
     uint32_t heads[SEG ? Q : 1][G][kHeadWords];  // bit b of word w: element 32w+b is a segment head
     uint32_t sample[SEG ? 1024 : 1];             // offsets[j * sample_stride], to start head searches
@@ -254,7 +259,9 @@ constexpr size_t seg_smem_bytes() {
 template <class Op, int RW>
 struct SegShape {
     static constexpr int kLookbackWarps = 3;
-    static constexpr int kThreads = 32 * (4 + kLookbackWarps + 2 * RW);
+    // R-loader, S-loader, storer, head warp, lookback warps, aggregator,
+    // reduce warps, finalize warps.
+    static constexpr int kThreads = 32 * (5 + kLookbackWarps + 2 * RW);
 };
 
 template <class Op, int RW, int RS, int SS, int Q, int G, bool INCL, bool SEG>
@@ -275,7 +282,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
     constexpr uint32_t NROLE = RW * 32;
     constexpr uint32_t ROWS = 128;  // rows per tile
     constexpr uint32_t LW = SegShape<Op, RW>::kLookbackWarps;
-    constexpr uint32_t kWarpLookback = 4, kWarpReduce = 4 + LW, kWarpFinal = 4 + LW + RW;
+    constexpr uint32_t kWarpLookback = 4, kWarpAgg = 4 + LW, kWarpReduce = 5 + LW, kWarpFinal = 5 + LW + RW;
+    constexpr uint32_t kLaneEntries = G * RW;  // aggregator entries per lane
+    auto entry_at = [](uint32_t j) -> uint32_t { return j + j / kLaneEntries; };
     constexpr int kHeadWords = TILE / 32;
     static_assert((SPLIT == 1 || SPLIT == 2) && RW % 4 == 0, "4 or 8 warps per role");
     static_assert(NROLE / SPLIT == ROWS, "a tile is one box of 128 rows of 128 bytes");
@@ -320,6 +329,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
         for (int q = 0; q < Q; ++q) {
             ptx::mbar_init(&ctrl->uknown[q], 1);
             ptx::mbar_init(&ctrl->uheads[q], 1);
+            ptx::mbar_init(&ctrl->uentries[q], RW);
             ptx::mbar_init(&ctrl->ureduced[q], 1);
             ptx::mbar_init(&ctrl->uprefix[q], 1);
             ptx::mbar_init(&ctrl->ufree[q], RW);
@@ -644,7 +654,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
         }
     }
     // ======================================================== lookback
-    else if (warp < kWarpReduce) {
+    else if (warp < kWarpAgg) {
         ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
         int64_t own_prev = -1;
         C own_incl = Op::chain_zero();
@@ -695,14 +705,86 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             __syncwarp();
         }
     }
+    // ======================================================== aggregator
+    // Once per unit: scans the unit's thread aggregates (kLaneEntries per
+    // lane, a serial chain, then one warp scan of the lane totals),
+    // publishes the unit's aggregate, and leaves each thread's state before
+    // it within the unit in place of its aggregate.
+    else if (warp == kWarpAgg) {
+        ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
+        for (uint32_t i = 0;; ++i) {
+            const int q = static_cast<int>(i % Q);
+            const uint32_t ph = (i / Q) & 1u;
+            uint32_t state = 0;
+            if (lane == 0) {
+                const uint64_t deadline = ptx::global_timer_ns() + long_budget;
+                while (!ptx::mbar_try_wait(&ctrl->uentries[q], ph)) {
+                    if (ld_volatile_u32(&ctrl->end_seq) <= i) {
+                        state = 1;
+                        break;
+                    }
+                    if (ptx::global_timer_ns() > deadline) {
+                        state = 2;
+                        break;
+                    }
+                }
+            }
+            state = __shfl_sync(kFullMask, state, 0);
+            __syncwarp();
+            if (state != 0) {
+                if (lane == 0 && state == 2) raise_error(a.hdr, kErrPipelineTimeout);
+                break;
+            }
+            const uint32_t j0 = lane * kLaneEntries;
+            S x = Op::zero();
+            bool xf = false;
+#pragma unroll
+            for (uint32_t m = 0; m < kLaneEntries; ++m) {
+                const S v = ctrl->tpre[q][entry_at(j0 + m)];
+                const bool vf = SEG && ctrl->tflag[SEG ? q : 0][SEG ? j0 + m : 0] != 0;
+                seg_combine<Op>(x, xf, v, vf);
+            }
+            x = Op::norm(x);
+            S inc = x;
+            bool incf = xf;
+            warp_scan_incl<Op, SEG>(inc, incf, lane);
+            // The unit's aggregate goes out before the per-thread states.
+            const S unit_agg = Op::shfl(inc, 31);
+            const bool unit_flag = SEG && __shfl_sync(kFullMask, incf, 31);
+            if (lane == 0) {
+                const uint32_t u = ctrl->unit_of[q];
+                const C chain = Op::to_chain(Op::norm(unit_agg));
+                desc_store<Op>(desc, u, u == 0 ? kInclusive : kAggregate, unit_flag, epoch, chain);
+                ctrl->uagg[q] = chain;
+                ctrl->uflag[q] = unit_flag;
+            }
+            S lp = Op::shfl_up(inc, 1);
+            bool lpf = SEG ? __shfl_up_sync(kFullMask, incf, 1) : false;
+            if (lane == 0) {
+                lp = Op::zero();
+                lpf = false;
+            }
+            // Second pass over the lane's entries: each becomes the state
+            // before it, and the chain moves past it.
+#pragma unroll
+            for (uint32_t m = 0; m < kLaneEntries; ++m) {
+                const S v = ctrl->tpre[q][entry_at(j0 + m)];
+                const bool vf = SEG && ctrl->tflag[SEG ? q : 0][SEG ? j0 + m : 0] != 0;
+                ctrl->tpre[q][entry_at(j0 + m)] = Op::norm(lp);
+                if (SEG) ctrl->tflag[SEG ? q : 0][SEG ? j0 + m : 0] = lpf ? 1 : 0;
+                seg_combine<Op>(lp, lpf, v, vf);
+            }
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&ctrl->ureduced[q]);
+        }
+    }
     // ======================================================== reduce
+    // Each thread reduces its part of each tile and leaves the aggregate
+    // (and whether its items hold a segment head) for the aggregator; no
+    // warp scan and no barrier per tile.
     else if (warp < kWarpFinal) {
         const uint32_t r = tid - kWarpReduce * 32;
         const uint32_t rw = warp - kWarpReduce;
-        ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
-        // State of the unit so far (the same in every reduce thread).
-        S unit_agg = Op::zero();
-        bool unit_flag = false;
         for (uint32_t rn = 0;; ++rn) {
             const int s = static_cast<int>(rn % RS);
             const uint32_t i = rn / G;
@@ -715,81 +797,33 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             if (SEG && live && k == 0)
                 ok = ptx::mbar_try_wait(&ctrl->uheads[q], (i / Q) & 1u) ||
                      ptx::mbar_wait_bounded(&ctrl->uheads[q], (i / Q) & 1u, ptx::global_timer_ns() + long_budget);
-            T v[ITEMS];
-            load_row(rbuf + static_cast<size_t>(s) * TILE, live ? t : a.num_tiles, r, v);
-            const uint32_t hb = (SEG && live) ? head_bits(heads_of(q, k), r) : 0u;
-            // Thread aggregate, then the warp's inclusive scan of them; warps
-            // whose items hold no segment head take the flag-free path.
-            const bool heads_here = SEG && __any_sync(kFullMask, hb != 0u);
-            S wv;
-            bool wf;
-            if (heads_here) {
-                wv = thread_aggregate<Op, ITEMS, true>(v, hb);
-                wf = hb != 0u;
-                warp_scan_incl<Op, true>(wv, wf, lane);
-            } else {
-                wv = thread_aggregate<Op, ITEMS, false>(v, 0u);
-                wf = false;
-                warp_scan_incl<Op, false>(wv, wf, lane);
-            }
-            S xv = Op::shfl_up(wv, 1);
-            bool xf = SEG ? __shfl_up_sync(kFullMask, wf, 1) : false;
-            if (lane == 0) {
-                xv = Op::zero();
-                xf = false;
-            }
-            if (lane == 31) {
-                ctrl->r_wtot[rn & 1u][rw] = wv;
-                ctrl->r_wflag[rn & 1u][rw] = wf;
-            }
-            const bool stop = named_bar_or(1, NROLE, !live || !ok);
-            if (lane == 0 && live) ptx::mbar_arrive(&ctrl->rfree[s]);
-            if (stop) {
-                if (r == 0) {
+            if (!live || !__all_sync(kFullMask, ok)) {
+                if (lane == 0) {
                     if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
-                    *reinterpret_cast<volatile uint32_t*>(&ctrl->end_seq) = i;
+                    if (rw == 0) *reinterpret_cast<volatile uint32_t*>(&ctrl->end_seq) = i;
                 }
                 break;
             }
-            // The state before this thread within the unit, for the scan
-            // pass; then the unit state moves past the tile.
-            S pre = unit_agg;
-            bool pf = unit_flag;
-            S tile_agg = Op::zero();
-            bool tile_f = false;
-#pragma unroll
-            for (int w2 = 0; w2 < RW; ++w2) {
-                const S x = ctrl->r_wtot[rn & 1u][w2];
-                const bool xfl = ctrl->r_wflag[rn & 1u][w2] != 0;
-                if (static_cast<uint32_t>(w2) < rw) seg_combine<Op>(pre, pf, x, xfl);
-                seg_combine<Op>(tile_agg, tile_f, x, xfl);
-            }
-            seg_combine<Op>(pre, pf, xv, xf);
-            ctrl->tpre[q][k][r] = Op::norm(pre);
-            if (SEG) {
-                const uint32_t fb = __ballot_sync(kFullMask, pf);
-                if (lane == 0) ctrl->tflag[q][k][rw] = fb;
-            }
-            seg_combine<Op>(unit_agg, unit_flag, tile_agg, tile_f);
-            unit_agg = Op::norm(unit_agg);
+            T v[ITEMS];
+            load_row(rbuf + static_cast<size_t>(s) * TILE, t, r, v);
+            const uint32_t hb = SEG ? head_bits(heads_of(q, k), r) : 0u;
+            const S agg = (SEG && __any_sync(kFullMask, hb != 0u)) ? thread_aggregate<Op, ITEMS, true>(v, hb)
+                                                                   : thread_aggregate<Op, ITEMS, false>(v, 0u);
+            // Every value of the warp's rows is in registers now.
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&ctrl->rfree[s]);
+            const uint32_t j = static_cast<uint32_t>(k) * NROLE + r;
+            ctrl->tpre[q][entry_at(j)] = agg;
+            if (SEG) ctrl->tflag[SEG ? q : 0][SEG ? j : 0] = hb != 0u ? 1 : 0;
             if (k == G - 1) {
-                if (r == 0) {
-                    const uint32_t u = t / G;
-                    const C chain = Op::to_chain(unit_agg);
-                    desc_store<Op>(desc, u, u == 0 ? kInclusive : kAggregate, unit_flag, epoch, chain);
-                    ctrl->uagg[q] = chain;
-                    ctrl->uflag[q] = unit_flag;
-                    ptx::mbar_arrive(&ctrl->ureduced[q]);
-                }
-                unit_agg = Op::zero();
-                unit_flag = false;
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&ctrl->uentries[q]);
             }
         }
     }
     // ======================================================== finalize
     else {
         const uint32_t f = tid - kWarpFinal * 32;
-        const uint32_t fw = warp - kWarpFinal;
         S run = Op::zero();  // the unit's prefix from the lookback
         for (uint32_t sn = 0;; ++sn) {
             const int s = static_cast<int>(sn % SS);
@@ -818,8 +852,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                 run = Op::from_chain(ctrl->upre[q]);
             }
             const uint32_t hb = SEG ? head_bits(heads_of(q, k), f) : 0u;
-            const S pre = ctrl->tpre[q][k][f];
-            const bool pf = SEG && ((ctrl->tflag[q][k][fw] >> lane) & 1u);
+            const uint32_t j = static_cast<uint32_t>(k) * NROLE + f;
+            const S pre = ctrl->tpre[q][entry_at(j)];
+            const bool pf = SEG && ctrl->tflag[SEG ? q : 0][SEG ? j : 0] != 0;
             const S base = pf ? pre : Op::combine(run, pre);
             if (SEG && __any_sync(kFullMask, hb != 0u))
                 thread_outputs<Op, ITEMS, true, INCL>(v, base, hb);
