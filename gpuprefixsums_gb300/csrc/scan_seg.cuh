@@ -225,7 +225,7 @@ struct SegCtrl {
     static constexpr int kHeadWords = 16384 / static_cast<int>(sizeof(typename Op::T)) / 32;
     uint64_t rfull[RS], rfree[RS];
     uint64_t sfull[SS], sdone[SS], sfree[SS];
-    uint64_t uknown[Q], uheads[Q], uentries[Q], ureduced[Q], uprefix[Q], ufree[Q];
+    uint64_t uknown[Q], uheads[Q], uentries[Q], ureduced[Q], ustates[Q], uprefix[Q], ufree[Q];
     uint32_t r_tile[RS];
     uint32_t s_tile[SS];
     uint32_t unit_of[Q];
@@ -330,6 +330,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             ptx::mbar_init(&ctrl->uknown[q], 1);
             ptx::mbar_init(&ctrl->uheads[q], 1);
             ptx::mbar_init(&ctrl->uentries[q], RW);
+            ptx::mbar_init(&ctrl->ustates[q], 1);
             ptx::mbar_init(&ctrl->ureduced[q], 1);
             ptx::mbar_init(&ctrl->uprefix[q], 1);
             ptx::mbar_init(&ctrl->ufree[q], RW);
@@ -708,8 +709,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
     // ======================================================== aggregator
     // Once per unit: scans the unit's thread aggregates (kLaneEntries per
     // lane, a serial chain, then one warp scan of the lane totals),
-    // publishes the unit's aggregate, and leaves each thread's state before
-    // it within the unit in place of its aggregate.
+    // publishes the unit's aggregate (ureduced: the lookback warp may
+    // publish the inclusive prefix), then leaves each thread's state before
+    // it within the unit in place of its aggregate (ustates).
     else if (warp == kWarpAgg) {
         ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
         for (uint32_t i = 0;; ++i) {
@@ -757,6 +759,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                 desc_store<Op>(desc, u, u == 0 ? kInclusive : kAggregate, unit_flag, epoch, chain);
                 ctrl->uagg[q] = chain;
                 ctrl->uflag[q] = unit_flag;
+                ptx::mbar_arrive(&ctrl->ureduced[q]);
             }
             S lp = Op::shfl_up(inc, 1);
             bool lpf = SEG ? __shfl_up_sync(kFullMask, incf, 1) : false;
@@ -770,12 +773,12 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             for (uint32_t m = 0; m < kLaneEntries; ++m) {
                 const S v = ctrl->tpre[q][entry_at(j0 + m)];
                 const bool vf = SEG && ctrl->tflag[SEG ? q : 0][SEG ? j0 + m : 0] != 0;
-                ctrl->tpre[q][entry_at(j0 + m)] = Op::norm(lp);
+                ctrl->tpre[q][entry_at(j0 + m)] = lp;
                 if (SEG) ctrl->tflag[SEG ? q : 0][SEG ? j0 + m : 0] = lpf ? 1 : 0;
                 seg_combine<Op>(lp, lpf, v, vf);
             }
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&ctrl->ureduced[q]);
+            if (lane == 0) ptx::mbar_arrive(&ctrl->ustates[q]);
         }
     }
     // ======================================================== reduce
@@ -843,10 +846,13 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             T v[ITEMS];
             load_row(sb, t, f, v);
             if (k == 0) {
-                // The unit's prefix; it also orders this warp after the head
-                // warp's bits and the reduce pass's per-thread prefixes.
+                // The unit's prefix (which also orders this warp after the
+                // head warp's bits), and the per-thread states (ustates).
                 bool pok = ptx::mbar_try_wait(&ctrl->uprefix[q], (i / Q) & 1u) ||
                            ptx::mbar_wait_bounded(&ctrl->uprefix[q], (i / Q) & 1u, ptx::global_timer_ns() + long_budget);
+                pok = pok && (ptx::mbar_try_wait(&ctrl->ustates[q], (i / Q) & 1u) ||
+                              ptx::mbar_wait_bounded(&ctrl->ustates[q], (i / Q) & 1u,
+                                                     ptx::global_timer_ns() + long_budget));
                 pok = __all_sync(kFullMask, pok);
                 if (!pok && lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
                 run = Op::from_chain(ctrl->upre[q]);
