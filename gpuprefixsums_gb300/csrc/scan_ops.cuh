@@ -44,6 +44,7 @@ struct OpInt {
     using C = U;
     static constexpr bool kL2Prefetch = true;
     static constexpr int kSplit = 1;
+    static constexpr bool kPackedRowSum = false;
     __device__ static S zero() { return 0; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
@@ -76,6 +77,7 @@ struct OpF32 {
     using C = float;
     static constexpr bool kL2Prefetch = true;
     static constexpr int kSplit = 1;
+    static constexpr bool kPackedRowSum = false;
     __device__ static S zero() { return 0.0f; }
     __device__ static S lift(T x) { return x; }
     __device__ static S add(S a, S b) { return a + b; }
@@ -114,6 +116,27 @@ struct F2 {
     float hi, lo;
 };
 
+// Two FP32 lanes in one 64-bit register for the packed add.rn.f32x2 /
+// sub.rn.f32x2 instructions (two IEEE round-to-nearest operations each).
+__device__ __forceinline__ uint64_t f2_pack(float a, float b) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t d, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(d));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 struct OpF32C {
     using T = float;
     using S = F2;
@@ -123,6 +146,9 @@ struct OpF32C {
     // warps of 16 items -- measured 25% slower on GB300: the per-thread
     // prefixes double and leave room for fewer stages.)
     static constexpr int kSplit = 1;
+    // The reduce pass sums a row as two half-chains (even and odd items) in
+    // packed FP32x2 TwoSums: half the instructions of one chain.
+    static constexpr bool kPackedRowSum = true;
     __device__ static S zero() { return F2{0.0f, 0.0f}; }
     __device__ static S lift(T x) { return F2{x, 0.0f}; }
     __device__ static S add(S a, S b) {
@@ -152,6 +178,27 @@ struct OpF32C {
         return F2{s, (a.hi - (s - bb)) + (a.lo - bb)};
     }
     __device__ static T out(S s) { return s.hi + s.lo; }
+    // Aggregate of N items (N even) without segment heads: TwoSum on the
+    // pairs (even item, odd item) of two independent chains at once, the
+    // errors of each chain summed lazily, then the two chains combined.
+    template <int N>
+    __device__ static S row_sum(const float (&v)[N]) {
+        static_assert(N % 2 == 0, "pairs of items");
+        uint64_t hi = f2_pack(0.0f, 0.0f), lo = hi;
+#pragma unroll
+        for (int m = 0; m < N / 2; ++m) {
+            const uint64_t x = f2_pack(v[2 * m], v[2 * m + 1]);
+            const uint64_t s = f2_add(hi, x);
+            const uint64_t bb = f2_sub(s, hi);
+            const uint64_t e = f2_add(f2_sub(hi, f2_sub(s, bb)), f2_sub(x, bb));
+            lo = f2_add(lo, e);
+            hi = s;
+        }
+        F2 a, b;
+        f2_unpack(hi, a.hi, b.hi);
+        f2_unpack(lo, a.lo, b.lo);
+        return norm(combine(a, b));
+    }
     __device__ static C to_chain(S s) { return static_cast<double>(s.hi) + static_cast<double>(s.lo); }
     __device__ static S from_chain(C c) {
         const float hi = static_cast<float>(c);
@@ -186,6 +233,7 @@ struct OpU32x4 {
     using C = uint4;
     static constexpr bool kL2Prefetch = true;
     static constexpr int kSplit = 1;
+    static constexpr bool kPackedRowSum = false;
     static constexpr int kDescWords = 2;
     __device__ static S zero() { return make_uint4(0u, 0u, 0u, 0u); }
     __device__ static S lift(T x) { return x; }

@@ -77,6 +77,7 @@ __device__ __forceinline__ void warp_scan_incl(typename Op::S& s, bool& f, uint3
 // scan, see scan_ops.cuh).
 template <class Op, int ITEMS, bool HEADS>
 __device__ __forceinline__ typename Op::S thread_aggregate(const typename Op::T (&v)[ITEMS], uint32_t hb) {
+    if constexpr (!HEADS && Op::kPackedRowSum) return Op::template row_sum<ITEMS>(v);
     typename Op::S x = Op::zero();
 #pragma unroll
     for (int e = 0; e < ITEMS; ++e) x = (HEADS && ((hb >> e) & 1u)) ? Op::lift(v[e]) : Op::acc(x, v[e]);
