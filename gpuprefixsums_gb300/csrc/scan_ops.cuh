@@ -33,16 +33,12 @@ template <>
 __device__ __forceinline__ float shfl_up_any(float s, uint32_t d) { return __shfl_up_sync(0xFFFFFFFFu, s, d); }
 
 // ------------------------------------------------------------- integers
-// kL2Prefetch: the kernel prefetches each unit into L2 when it takes the
-// unit (pays off for the streaming-bound operations, measured 3-4% on GB300;
-// the compensated scan is bound by its arithmetic and loses 4% instead).
 // kSplit: threads per 128-byte row of a tile (1: 4 + 4 compute warps).
 template <typename U>
 struct OpInt {
     using T = U;
     using S = U;
     using C = U;
-    static constexpr bool kL2Prefetch = true;
     static constexpr int kSplit = 1;
     static constexpr bool kPackedRowSum = false;
     __device__ static S zero() { return 0; }
@@ -75,7 +71,6 @@ struct OpF32 {
     using T = float;
     using S = float;
     using C = float;
-    static constexpr bool kL2Prefetch = true;
     static constexpr int kSplit = 1;
     static constexpr bool kPackedRowSum = false;
     __device__ static S zero() { return 0.0f; }
@@ -141,7 +136,6 @@ struct OpF32C {
     using T = float;
     using S = F2;
     using C = double;
-    static constexpr bool kL2Prefetch = false;
     // One thread per 128-byte row. (Two per row -- 8 reduce and 8 finalize
     // warps of 16 items -- measured 25% slower on GB300: the per-thread
     // prefixes double and leave room for fewer stages.)
@@ -231,7 +225,6 @@ struct OpU32x4 {
     using T = uint4;
     using S = uint4;
     using C = uint4;
-    static constexpr bool kL2Prefetch = true;
     static constexpr int kSplit = 1;
     static constexpr bool kPackedRowSum = false;
     static constexpr int kDescWords = 2;
