@@ -395,23 +395,66 @@ def run_struct(stream, copy_gbs, reps=20):
     return res
 
 
+def graph_us(fn, stream, k):
+    """GPU time per call of fn (which launches on `stream`): k calls captured
+    in one CUDA graph, the graph replayed 5 times, CUDA events around the
+    replays -- the host's launch rate does not enter, unlike a Python loop of
+    launches at small sizes."""
+    import torch
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            fn()
+        stream.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(k):
+                fn()
+        g.replay()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(5):
+            g.replay()
+        stop.record(stream)
+        stop.synchronize()
+    return start.elapsed_time(stop) * 1e3 / (5 * k)
+
+
 def run_sweep(stream, d_in, d_out):
     """Config-2 sizes: u32 exclusive chained scan at n = 2^10 .. 2^28 (every
-    second power of two) on the benchmark's buffers, and u64 at n = 2^27.
-    Inputs below about 2^24 elements stay in L2 between launches."""
+    second power of two) on the benchmark's buffers, beside CUB DeviceScan on
+    the same buffers, and u64 at n = 2^27. GPU time per scan from CUDA-graph
+    replay. Inputs below about 2^24 elements stay in L2 between launches.
+    The plan's defaults pick the kernel: one CTA up to 64 KB, one tile per
+    CTA up to 4 MB, the persistent L2-buffered kernel above."""
     import torch
 
     from gpuprefixsums_gb300 import Plan
-    res = {"workload": "u32 exclusive chained scan by size (L2-resident below ~2^24), u64 exclusive at 2^27",
-           "u32_gbs": {}}
+    from gpuprefixsums_gb300 import build as gbuild
+    res = {"workload": "u32 exclusive chained scan by size (L2-resident below ~2^24; GPU time per scan from "
+                       "CUDA-graph replay), u64 exclusive at 2^27",
+           "u32": {}}
+    cub = None
+    try:
+        cub = ctypes.CDLL(gbuild.build_cub_compare())
+        cub.gps_cub_scan_u32.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]
+        tb = ctypes.c_size_t(0)
+        cub.gps_cub_scan_u32(0, d_in.data_ptr(), d_out.data_ptr(), d_in.numel(), None, ctypes.byref(tb), None)
+        temp = torch.empty(max(1, tb.value), dtype=torch.uint8, device="cuda")
+    except Exception as e:  # comparison only
+        res["cub_error"] = str(e)[:200]
+    sp = ctypes.c_void_p(stream.cuda_stream)
     with Plan("csdl", "u32", max_n=d_in.numel()) as plan:
         for k in range(10, 29, 2):
             n = 1 << k
-            step = lambda: plan.scan(d_in, d_out, n=n, stream=stream)  # noqa: E731
-            for _ in range(3):
-                step()
-            ms = time_loop(step, max(20, min(2000, (1 << 30) // n)), stream)
-            res["u32_gbs"][f"2^{k}"] = {"gbs": round(n * 8 / (ms * 1e-3) / 1e9, 2), "us": round(ms * 1e3, 2)}
+            reps = max(4, min(50, (1 << 26) // n))
+            us = graph_us(lambda: plan.scan(d_in, d_out, n=n, stream=stream), stream, reps)
+            row = {"gbs": round(n * 8 / (us * 1e-6) / 1e9, 2), "us": round(us, 2)}
+            if cub is not None:
+                row["cub_us"] = round(graph_us(lambda: cub.gps_cub_scan_u32(0, d_in.data_ptr(), d_out.data_ptr(), n,
+                                                                            temp.data_ptr(), ctypes.byref(tb), sp),
+                                               stream, reps), 2)
+            res["u32"][f"2^{k}"] = row
         plan.check(stream)
     n64 = 1 << 27
     x64, o64 = d_in.view(torch.int64)[:n64], d_out.view(torch.int64)[:n64]

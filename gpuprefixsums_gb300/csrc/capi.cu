@@ -50,6 +50,7 @@ struct gps_plan_s {
     void* desc16;
     // Integer scans of at most this many elements run in one CTA (small.cu).
     uint64_t small_max;
+    uint64_t mid_max;  // chained-scan plans: largest scan run as one tile per CTA
     // Autotuned launch configuration of the generic kernel per [segmented?]
     // [size class] (index into gps::kGenericCandidates; -1: not tuned).
     int8_t tuned[2][kSizeClasses];
@@ -151,6 +152,8 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
                              &p->last_launch);
     } else if (n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
         err = gps::launch_small(p->dtype, inclusive, a, stream, &p->last_launch);
+    } else if (p->algo == GPS_ALGO_CSDL && n <= p->mid_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
+        err = gps::launch_mid(p->dtype, inclusive, a, p->num_sms, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
         err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0 || p->stall.fallback_polls != 0, a, p->num_sms,
                                stream, &p->last_launch);
@@ -216,6 +219,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->wait_budget_ns = kDefaultBudgetNs;
     std::memset(p->tuned, -1, sizeof(p->tuned));
     p->small_max = gps::small_scan_max_elems(dtype);
+    p->mid_max = algo == GPS_ALGO_CSDL && !generic_only(dtype) ? gps::kMidMaxBytes / gps::dtype_size(dtype) : 0;
     cudaError_t err = cudaGetDevice(&p->device);
     if (err == cudaSuccess) err = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (err != cudaSuccess) {
@@ -620,6 +624,14 @@ gps_status gps_plan_geometry(gps_plan p, uint64_t n, uint32_t* tile_elems, uint3
     if (grid) *grid = static_cast<uint32_t>(p->last_launch.grid);
     const bool small = !generic_only(p->dtype) && n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0;
     if (launches) *launches = n == 0 ? 0u : (small || p->algo == GPS_ALGO_CSDL ? 1u : 3u);
+    return GPS_OK;
+}
+
+gps_status gps_plan_set_mid_max(gps_plan p, uint64_t max_n) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (max_n != 0 && (p->algo != GPS_ALGO_CSDL || generic_only(p->dtype)))
+        return fail(GPS_ERR_UNSUPPORTED, "the one-tile-per-CTA scan runs integer chained-scan plans only");
+    p->mid_max = max_n;
     return GPS_OK;
 }
 

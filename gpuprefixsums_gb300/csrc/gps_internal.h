@@ -162,6 +162,14 @@ constexpr size_t kSmallMaxBytes = 64 * 1024;
 uint64_t small_scan_max_elems(gps_dtype dtype);
 cudaError_t launch_small(gps_dtype dtype, bool inclusive, const ScanArgs& a, cudaStream_t stream, LaunchInfo* info);
 
+// Mid-size integer chained scans, one 16 KB tile per CTA (mid.cu); the
+// default upper size of a plan, in bytes of input (measured on GB300: one
+// tile per CTA is faster than the persistent kernel up to 2^20 u32, 7.7
+// against 10.4 us, and slower from 2^21 on, 15.0 against 12.1 us).
+constexpr size_t kMidMaxBytes = 4ull << 20;
+cudaError_t launch_mid(gps_dtype dtype, bool inclusive, const ScanArgs& a, int num_sms, cudaStream_t stream,
+                       LaunchInfo* info);
+
 uint32_t csdl_tile_elems(gps_dtype dtype);
 // Sets the text gps_last_error() returns on this host thread.
 void record_error(const char* msg);

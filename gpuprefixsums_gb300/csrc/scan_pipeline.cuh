@@ -183,8 +183,9 @@ constexpr int lookback_per_lane() {
 // slot holds an aggregate; a window of aggregates only moves it back by 32*K
 // slots. Slots >= u count as empty aggregates. A poll that finds a needed
 // slot not ready re-reads only the pairs holding such slots, after an
-// exponential back-off. Bounded by the wait budget.
-template <typename T, int SPAN, bool STALL>
+// exponential back-off (from poll SPIN on; the polls before it re-read at
+// once). Bounded by the wait budget.
+template <typename T, int SPAN, bool STALL, uint32_t SPIN = 0>
 __device__ T lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane, T carry, int64_t bound,
                       T bound_val) {
     using D = DescTraits<T>;
@@ -310,8 +311,10 @@ __device__ T lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t la
                     return prefix;
                 }
             }
-            __nanosleep(backoff);
-            backoff = backoff < 1024 ? backoff * 2 : 1024;
+            if (polls > SPIN) {
+                __nanosleep(backoff);
+                backoff = backoff < 1024 ? backoff * 2 : 1024;
+            }
         }
     }
 }

@@ -188,6 +188,11 @@ class Plan:
         """Largest integer scan run in one CTA (0: always the multi-CTA kernels)."""
         check(lib.gps_plan_set_small_max(self._h, int(max_n)), "gps_plan_set_small_max")
 
+    def set_mid_max(self, max_n: int) -> None:
+        """Largest integer chained scan run as one tile per CTA (0: always the
+        persistent kernel above the one-CTA size)."""
+        check(lib.gps_plan_set_mid_max(self._h, int(max_n)), "gps_plan_set_mid_max")
+
     def stats(self, stream=None) -> dict:
         s = _lib.LookbackStats()
         check(lib.gps_plan_stats(self._h, ctypes.c_void_p(_stream_handle(stream)), ctypes.byref(s)), "gps_plan_stats")

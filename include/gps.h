@@ -228,6 +228,15 @@ gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
  * kernels. Forced-stall and fallback modes always use the multi-CTA kernels. */
 gps_status gps_plan_set_small_max(gps_plan plan, uint64_t max_n);
 
+/* Integer scans on a GPS_ALGO_CSDL plan above the one-CTA size and of at
+ * most max_n elements (default: 4 MB of input, 2^20 u32 or 2^19 u64) run
+ * as one 16 KB tile per CTA -- a single-pass chained scan without the
+ * persistent kernel's pipeline, whose latency dominates at these sizes;
+ * larger ones run on the persistent L2-buffered kernel. 0 sends them all to
+ * the persistent kernel. Forced-stall and fallback modes always use the
+ * persistent kernel. */
+gps_status gps_plan_set_mid_max(gps_plan plan, uint64_t max_n);
+
 /* Lookback statistics gathered while forced-stall mode is on. Synchronizes
  * `stream`. */
 typedef struct gps_lookback_stats {

@@ -19,6 +19,22 @@ NP = {"u32": np.uint32, "u64": np.uint64}
 TORCH_VIEW = {"u32": (np.int32, torch.int32), "u64": (np.int64, torch.int64)}
 
 
+# Kernel paths of an integer scan: the one-CTA scan of small inputs, the
+# one-tile-per-CTA chained scan of mid sizes, and the persistent kernels.
+PATHS = ["one_cta", "mid", "persistent"]
+
+
+def use_path(plan, algo, path):
+    """Route every size of the test through one kernel path (the defaults
+    send each size to the path its size class takes)."""
+    if path == "mid" and algo != "csdl":
+        pytest.skip("the mid-size kernel serves chained-scan plans")
+    if path != "one_cta":
+        plan.set_small_max(0)
+    if path == "persistent":
+        plan.set_mid_max(0)
+
+
 def to_dev(x: np.ndarray) -> torch.Tensor:
     view = np.int32 if x.dtype == np.uint32 else np.int64
     return torch.from_numpy(np.ascontiguousarray(x).view(view)).cuda()
@@ -52,15 +68,14 @@ def test_config1_2pow20_uniform_0_15(cuda, algo, inclusive):
 # -------------------------------------------- the reference's size sweep
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("inclusive", [False, True])
-@pytest.mark.parametrize("one_cta", [True, False])
-def test_every_size_from_one_to_two_tiles_all_ones_in_place(cuda, algo, inclusive, one_cta):
+@pytest.mark.parametrize("path", PATHS)
+def test_every_size_from_one_to_two_tiles_all_ones_in_place(cuda, algo, inclusive, path):
     # ChainedScanDecoupledLookbackDispatcher.cuh:48-59: every n in
     # [4096, 8192] on all-ones input, scanned in place; extended down to 1.
-    # Both through the one-CTA scan of small inputs and with it turned off.
+    # Through each kernel path.
     top = 2 * 4096 + 1
     with Plan(algo, "u32", max_n=top) as plan:
-        if not one_cta:
-            plan.set_small_max(0)
+        use_path(plan, algo, path)
         buf = torch.empty(top, dtype=torch.int32, device="cuda")
         ar = torch.arange(top + 1, dtype=torch.int64, device="cuda")
         bad = []
@@ -77,8 +92,8 @@ def test_every_size_from_one_to_two_tiles_all_ones_in_place(cuda, algo, inclusiv
 @pytest.mark.parametrize("dtype", ["u32", "u64"])
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("inclusive", [False, True])
-@pytest.mark.parametrize("one_cta", [True, False])
-def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive, one_cta):
+@pytest.mark.parametrize("path", PATHS)
+def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive, path):
     # Full-range values (sums wrap), out of place, and words after n must
     # stay untouched (the reference writes up to align4(n)).
     rng = np.random.default_rng(99)
@@ -87,8 +102,7 @@ def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive, one_c
                        rng.integers(1, 40 * t, size=12).tolist()))
     canary = 64
     with Plan(algo, dtype, max_n=max(sizes)) as plan:
-        if not one_cta:
-            plan.set_small_max(0)
+        use_path(plan, algo, path)
         for n in sizes:
             x = rand(dtype, n, seed=n)
             d_in = to_dev(x)
@@ -103,8 +117,8 @@ def test_random_sizes_full_range_with_canary(cuda, dtype, algo, inclusive, one_c
 
 @pytest.mark.parametrize("dtype", ["u32", "u64"])
 @pytest.mark.parametrize("algo", ALGOS)
-@pytest.mark.parametrize("one_cta", [True, False])
-def test_unaligned_pointers_take_the_plain_path(cuda, dtype, algo, one_cta):
+@pytest.mark.parametrize("path", PATHS)
+def test_unaligned_pointers_take_the_plain_path(cuda, dtype, algo, path):
     # Pointers aligned to the element but not to 16 bytes; in and out offset
     # differently.
     es = 4 if dtype == "u32" else 8
@@ -115,8 +129,7 @@ def test_unaligned_pointers_take_the_plain_path(cuda, dtype, algo, one_cta):
         big_out = torch.zeros(n + 8, dtype=TORCH_VIEW[dtype][1], device="cuda")
         big_in[1:n + 1] = to_dev(x)
         with Plan(algo, dtype, max_n=n) as plan:
-            if not one_cta:
-                plan.set_small_max(0)
+            use_path(plan, algo, path)
             plan.scan_ptr(big_in.data_ptr() + es, big_out.data_ptr() + 3 * es, n, inclusive=False)
             plan.check()
         got = to_host(big_out[3:n + 3], NP[dtype])
@@ -178,17 +191,20 @@ def test_config2_exclusive_sweep_2pow10_to_2pow28(cuda, dist):
 # ------------------------------------------------------------ host arrays
 @pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("inclusive", [False, True])
-def test_host_array_scan_chunks_and_carries(cuda, algo, inclusive):
+@pytest.mark.parametrize("path", ["mid", "persistent"])
+def test_host_array_scan_chunks_and_carries(cuda, algo, inclusive, path):
     n = (1 << 23) + 12345  # the plan's 2^21 bound forces five chunks
     x = rand("u32", n, seed=5)
     h_in = torch.from_numpy(x.view(np.int32)).pin_memory()
     h_out = torch.empty(n, dtype=torch.int32).pin_memory()
     with Plan(algo, "u32", max_n=1 << 21) as plan:
+        use_path(plan, algo, path)
         plan.scan_host(h_in.data_ptr(), h_out.data_ptr(), n, inclusive=inclusive)
         plan.check()
     assert oracle.validate(x, h_out.numpy().view(np.uint32), inclusive) == 0
     # in place on the host
     with Plan(algo, "u32", max_n=1 << 21) as plan:
+        use_path(plan, algo, path)
         plan.scan_host(h_in.data_ptr(), h_in.data_ptr(), n, inclusive=inclusive)
     assert oracle.validate(x, h_in.numpy().view(np.uint32), inclusive) == 0
 
@@ -206,13 +222,15 @@ def test_many_consecutive_launches_reuse_the_workspace(cuda):
 
 
 @pytest.mark.parametrize("algo", ALGOS)
-def test_cuda_graph_capture_and_replay(cuda, algo):
+@pytest.mark.parametrize("path", ["mid", "persistent"])
+def test_cuda_graph_capture_and_replay(cuda, algo, path):
     n = 3_000_001
     x = rand("u32", n, seed=77)
     d_in = to_dev(x)
     d_out = torch.empty_like(d_in)
     ref = oracle.scan(x, inclusive=True)
     with Plan(algo, "u32", max_n=n) as plan:
+        use_path(plan, algo, path)
         plan.scan(d_in, d_out, inclusive=True)  # warm-up outside capture
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
@@ -397,3 +415,29 @@ def test_reference_csdl_30_bit_descriptor_limit(cuda):
     assert np.all(diff % (1 << 30) == 0)
     assert np.array_equal(theirs[:4096], want[:4096])  # tile 0 needs no descriptor
     assert np.any(diff != 0)
+
+
+# ------------------------------------------------------ kernel selection
+def test_mid_size_scans_take_one_tile_per_cta(cuda):
+    # Above the one-CTA size and up to the plan's mid size, a chained scan
+    # launches one CTA per 16 KB tile; past it, the persistent kernel.
+    n = (1 << 20) - 7
+    x = rand("u32", n, seed=41)
+    with Plan("csdl", "u32", max_n=n) as plan:
+        out = plan.scan(to_dev(x))
+        assert plan.geometry(n)["grid"] == (n + 4095) // 4096
+        assert oracle.validate(x, to_host(out, np.uint32), False) == 0
+        plan.set_mid_max(1 << 16)
+        out = plan.scan(to_dev(x))
+        assert plan.geometry(n)["grid"] <= 2 * torch.cuda.get_device_properties(0).multi_processor_count
+        assert oracle.validate(x, to_host(out, np.uint32), False) == 0
+        plan.check()
+
+
+def test_mid_max_takes_integer_chained_scan_plans_only(cuda):
+    for algo, dtype in (("rts", "u32"), ("csdl", "f32"), ("csdl", "u32x4")):
+        with Plan(algo, dtype, max_n=1024) as plan:
+            plan.set_mid_max(0)
+            with pytest.raises(GpsError) as e:
+                plan.set_mid_max(1024)
+            assert e.value.status == _lib.GPS_ERR_UNSUPPORTED
