@@ -351,14 +351,15 @@ struct __align__(16) Chunk {
     T v[16 / sizeof(T)];
 };
 
-// Logical exclusive prefix of each of the 8 chunks a thread holds in rotated
-// order: register j holds chunk (j + rot) & 7, so chunk 0 sits in register
-// (8 - rot) & 7. With wrapping integer arithmetic the prefix of register j is
-// Q[j] - Q[start], plus the thread total when register j comes before start.
+// Logical exclusive prefix of each of the CHUNKS chunks (a power of two) a
+// thread holds in rotated order: register j holds chunk (j + rot) % CHUNKS,
+// so chunk 0 sits in register (CHUNKS - rot) % CHUNKS. With wrapping integer
+// arithmetic the prefix of register j is Q[j] - Q[start], plus the thread
+// total when register j comes before start.
 template <typename T, int CHUNKS>
 __device__ __forceinline__ void rotated_chunk_prefix(const T (&cs)[CHUNKS], uint32_t rot, T (&cpre)[CHUNKS],
                                                      T& total) {
-    static_assert(CHUNKS == 8, "eight 16-byte chunks per thread");
+    static_assert(CHUNKS >= 2 && (CHUNKS & (CHUNKS - 1)) == 0, "a power of two of 16-byte chunks per thread");
     T q[CHUNKS];
     T run = 0;
 #pragma unroll
