@@ -18,8 +18,9 @@
 //      re-polling without back-off for the first polls: the predecessors'
 //      descriptors are typically microseconds away, not a unit's pipeline);
 //   4. publish the inclusive prefix, add the prefix, store.
-// The last CTA to finish resets the counters and advances the epoch, as the
-// L2 kernel does, so the two kernels share a plan's scratch.
+// The last CTA to be done with the descriptors resets the counters and
+// advances the epoch, as the L2 kernel does, so the two kernels share a
+// plan's scratch.
 #include "gps_device.cuh"
 #include "gps_internal.h"
 #include "launch_util.h"
@@ -33,8 +34,8 @@ constexpr int kMidThreads = 256;
 // The last CTA to be done with the descriptors (its lookback finished and its
 // inclusive prefix published) returns the counters to zero and advances the
 // epoch, which retires every descriptor of this launch. Called by one thread
-// per CTA right after that point, before the CTA's output stores, which need
-// no ordering against it.
+// per CTA once its descriptor traffic is over; the output stores need no
+// ordering against it, so it runs while they drain.
 template <typename T>
 __device__ __forceinline__ void retire_launch(const ScanArgs& a, uint32_t epoch, bool block_ids) {
     using D = DescTraits<T>;
@@ -108,7 +109,6 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
             if (t != 0) D::store(desc + t, D::pack(kInclusive, epoch, pre + total));
             if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
             s_prefix = pre;
-            retire_launch<T>(a, epoch, block_ids);
         }
     }
     __syncthreads();
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
         for (int e = 0; e < ITEMS; ++e)
             if (i0 + e < a.n) out[i0 + e] = v[e];
     }
-
+    if (tid == 0) retire_launch<T>(a, epoch, block_ids);
 }
 
 // The same scan for 16-byte-aligned buffers, with the tile moved by one bulk
@@ -221,7 +221,6 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_bulk_kernel(const ScanArgs
             if (t != 0) D::store(desc + t, D::pack(kInclusive, epoch, pre + total));
             if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
             s_prefix = pre;
-            retire_launch<T>(a, epoch, block_ids);
         }
     }
     __syncthreads();
@@ -252,10 +251,12 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_bulk_kernel(const ScanArgs
         ptx::bulk_commit();
     }
     if (tid < cnt - bulk_elems) out[t0 + bulk_elems + tid] = tile[bulk_elems + tid];
-
-    // The store must have read the tile before the CTA's shared memory goes
-    // away.
-    if (tid == 0 && bulk) ptx::bulk_wait_read<0>();
+    if (tid == 0) {
+        retire_launch<T>(a, epoch, block_ids);
+        // The store must have read the tile before the CTA's shared memory
+        // goes away.
+        if (bulk) ptx::bulk_wait_read<0>();
+    }
 }
 
 template <typename T, bool INCL, bool VEC>
