@@ -13,11 +13,16 @@
 // inclusive prefix. Short segments therefore resolve inside their unit, long
 // ones walk back to the unit where they start. The reference has no batched
 // or floating-point scan; this kernel covers those rows of the design
-// (dtype per launch: u32, u64, plain FP32, compensated FP32).
+// (dtype per launch: u32, u64, plain FP32, compensated FP32, and structs of
+// four u32 members).
 //
 // Warps: 0 R-loader, 1 S-loader, 2 storer, 3 head warp (segment heads of each
-// unit, from the offsets), then LW lookback warps, RW reduce warps and RW
-// finalize warps; see scan_l2.cuh for the two passes.
+// unit, from the offsets), then LW lookback warps, the aggregator warp, RW
+// reduce warps and RW finalize warps; see scan_l2.cuh for the two passes.
+// Unlike scan_l2.cuh, the reduce warps only aggregate their rows: once per
+// unit the aggregator warp scans those aggregates, publishes the unit's
+// aggregate and hands every finalize thread its state within the unit, so
+// neither pass has a warp scan or a barrier per tile.
 #pragma once
 #include <type_traits>
 
