@@ -67,10 +67,11 @@ def parse_args():
     p.add_argument("--no-compare", action="store_true",
                    help="only the timed scans (for profiling): no copy/CUB/RTS/e2e/CPU legs")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, fp32 and mixed workloads")
-    p.add_argument("--profile-case", choices=["batched", "f32c", "select", "struct"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "f32c", "select", "struct", "mid"], default=None,
                    help="launch one small case three times and exit (ncu captures): 1024 of the batched "
                         "workload's segments, 2^26 compensated-f32 elements, a select of 2^26 u32 by "
-                        "Bernoulli(0.3) flags, or an inclusive scan of 2^24 structs of four u32")
+                        "Bernoulli(0.3) flags, an inclusive scan of 2^24 structs of four u32, or an "
+                        "exclusive u32 scan of 2^20 elements (the one-tile-per-CTA kernel)")
     p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
@@ -802,6 +803,13 @@ def run_profile_case(args):
                 out, cnt = plan.select(x, fl)
             plan.check()
         out = out[:int(cnt.item())]
+    elif args.profile_case == "mid":
+        n = 1 << 20
+        x = torch.randint(0, 256, (n,), dtype=torch.int32, device="cuda")
+        with Plan("csdl", "u32", max_n=n) as plan:
+            for _ in range(3):
+                out = plan.scan(x)
+            plan.check()
     elif args.profile_case == "struct":
         n = 1 << 24  # 256 MiB of structs
         x = torch.randint(-2 ** 31, 2 ** 31 - 1, (n, 4), dtype=torch.int32, device="cuda")
