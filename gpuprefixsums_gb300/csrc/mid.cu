@@ -10,8 +10,10 @@
 //      once (every CTA it may wait on is running), else from the plan's
 //      atomic counter (ids follow the order in which CTAs start, so a CTA
 //      only waits on CTAs already running);
-//   2. load 16 bytes x 4 per thread (16 u32 or 8 u64, consecutive), sum
-//      them, block-scan the thread sums (include/gps_device.cuh);
+//   2. load the tile (one bulk copy into shared memory for 16-byte-aligned
+//      buffers, else element by element); each thread sums its 64
+//      consecutive bytes (16 u32 or 8 u64) and the thread sums are
+//      block-scanned (include/gps_device.cuh);
 //   3. publish the tile aggregate, and let warp 0 walk back over the
 //      predecessors' descriptors (the same 8- or 16-byte descriptors, epoch
 //      and lookback as the L2 kernel: lookback() in scan_pipeline.cuh, here
@@ -56,11 +58,12 @@ __device__ __forceinline__ void retire_launch(const ScanArgs& a, uint32_t epoch,
     }
 }
 
-template <typename T, bool INCL, bool VEC>
+// Buffers not aligned to 16 bytes: each thread loads and stores its 64
+// bytes element by element.
+template <typename T, bool INCL>
 __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs a, bool block_ids) {
     constexpr int TILE = 16384 / static_cast<int>(sizeof(T));
     constexpr int ITEMS = TILE / kMidThreads;  // 16 u32 or 8 u64: 64 bytes
-    constexpr int EPV = 16 / static_cast<int>(sizeof(T));
     using D = DescTraits<T>;
     using word = typename D::word;
     __shared__ gps_device::BlockScanStorage<kMidThreads, T> st;
@@ -78,21 +81,10 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
     const T* in = static_cast<const T*>(a.in);
     T* out = static_cast<T*>(a.out);
     const uint64_t i0 = static_cast<uint64_t>(t) * TILE + static_cast<uint64_t>(tid) * ITEMS;
-    const bool whole = i0 + ITEMS <= a.n;
 
     T v[ITEMS];
-    if (VEC && whole) {
 #pragma unroll
-        for (int j = 0; j < ITEMS / EPV; ++j) {
-            const uint4 q = *reinterpret_cast<const uint4*>(in + i0 + j * EPV);
-            const T* qt = reinterpret_cast<const T*>(&q);
-#pragma unroll
-            for (int e = 0; e < EPV; ++e) v[j * EPV + e] = qt[e];
-        }
-    } else {
-#pragma unroll
-        for (int e = 0; e < ITEMS; ++e) v[e] = i0 + e < a.n ? in[i0 + e] : T(0);
-    }
+    for (int e = 0; e < ITEMS; ++e) v[e] = i0 + e < a.n ? in[i0 + e] : T(0);
     T sum = 0;
 #pragma unroll
     for (int e = 0; e < ITEMS; ++e) sum += v[e];
@@ -125,20 +117,9 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
             run += x;
         }
     }
-    if (VEC && whole) {
 #pragma unroll
-        for (int j = 0; j < ITEMS / EPV; ++j) {
-            uint4 q;
-            T* qt = reinterpret_cast<T*>(&q);
-#pragma unroll
-            for (int e = 0; e < EPV; ++e) qt[e] = v[j * EPV + e];
-            *reinterpret_cast<uint4*>(out + i0 + j * EPV) = q;
-        }
-    } else {
-#pragma unroll
-        for (int e = 0; e < ITEMS; ++e)
-            if (i0 + e < a.n) out[i0 + e] = v[e];
-    }
+    for (int e = 0; e < ITEMS; ++e)
+        if (i0 + e < a.n) out[i0 + e] = v[e];
     if (tid == 0) retire_launch<T>(a, epoch, block_ids);
 }
 
@@ -261,7 +242,7 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_bulk_kernel(const ScanArgs
 
 template <typename T, bool INCL, bool VEC>
 cudaError_t launch_mid_v(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
-    auto kern = VEC ? mid_bulk_kernel<T, INCL> : mid_scan_kernel<T, INCL, false>;
+    auto kern = VEC ? mid_bulk_kernel<T, INCL> : mid_scan_kernel<T, INCL>;
     int occ = 0;
     cudaError_t err = resident_ctas_per_sm(kern, kMidThreads, 0, &occ);
     if (err != cudaSuccess) return err;
