@@ -67,7 +67,18 @@ def test_plan_create_rejects_bad_arguments_before_any_cuda_call():
     assert lib.gps_plan_create(ctypes.byref(h), 0, 9, 10) == _lib.GPS_ERR_INVALID_ARGUMENT
     assert lib.gps_plan_create(ctypes.byref(h), 0, 0, 0) == _lib.GPS_ERR_INVALID_ARGUMENT
     assert lib.gps_plan_create(ctypes.byref(h), 0, 0, 1 << 60) == _lib.GPS_ERR_INVALID_ARGUMENT
+    # Floating-point and struct element types run on chained-scan plans only.
+    for dtype in (_lib.DTYPE_F32, _lib.DTYPE_F32_COMPENSATED, _lib.DTYPE_U32X4):
+        assert lib.gps_plan_create(ctypes.byref(h), _lib.ALGO_RTS, dtype, 1024) == _lib.GPS_ERR_UNSUPPORTED
     assert h.value is None
+
+
+def test_plan_setters_reject_a_null_plan_without_a_gpu():
+    from gpuprefixsums_gb300 import _lib, lib
+    for call in (lambda: lib.gps_plan_set_small_max(None, 0), lambda: lib.gps_plan_set_mid_max(None, 0),
+                 lambda: lib.gps_plan_set_fallback(None, 0), lambda: lib.gps_plan_set_wait_budget(None, 1000)):
+        assert call() == _lib.GPS_ERR_INVALID_ARGUMENT
+        assert b"plan is NULL" in lib.gps_last_error()
 
 
 def test_compat_selftest_was_built():
