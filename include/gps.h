@@ -139,8 +139,9 @@ gps_status gps_scan_segmented(gps_plan plan, gps_scan_kind kind, const void* d_i
  * flag byte d_flags[i] is non-zero, in their order, to d_out[0 .. count), and
  * writes count to *d_num_selected (uint64, device memory). One launch: the
  * flag scan is fused with the scatter, so the values and flags are read once
- * and only the selected values are written. Any GPS_ALGO_CSDL plan; the
- * element size is the plan's (4 bytes for u32 / f32, 8 for u64). d_in and
+ * and only the selected values are written. Any GPS_ALGO_CSDL plan but a
+ * struct one (GPS_DTYPE_U32X4: GPS_ERR_UNSUPPORTED); the element size is
+ * the plan's (4 bytes for u32 / f32, 8 for u64). d_in and
  * d_flags 16-byte aligned, d_out aligned to the element size and not
  * overlapping them; n <= max_n. Asynchronous on `stream`; capturable.
  * No counterpart in the reference; it is the scan's next consumer (the
@@ -181,7 +182,7 @@ gps_status gps_plan_set_generic_config(gps_plan plan, int segmented, uint64_t n,
  * should be pinned (cudaHostAlloc / cudaHostRegister) for full speed; h_in ==
  * h_out is allowed. n may exceed the plan's max_n: the plan only bounds the
  * chunk size. Device staging memory is allocated on first use and kept by
- * the plan. */
+ * the plan. u32 and u64 plans (others: GPS_ERR_UNSUPPORTED). */
 gps_status gps_scan_host(gps_plan plan, gps_scan_kind kind, const void* h_in, void* h_out,
                          uint64_t n, gps_stream_t stream);
 
