@@ -73,11 +73,31 @@ def parse_args():
                         "Bernoulli(0.3) flags, an inclusive scan of 2^24 structs of four u32, or an "
                         "exclusive u32 scan of 2^20 elements (the one-tile-per-CTA kernel)")
     p.add_argument("--e2e-steps", type=int, default=8)
+    p.add_argument("--clock-soak-s", type=float, default=1.0,
+                   help="seconds of untimed steps sampled for clocks right before the timed region")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
 
 
 # ----------------------------------------------------------------- helpers
+INPUT_SEED = 2028
+
+
+def workload_config(args, world):
+    """The workload both arms time, described identically: the same n, the
+    same values (numpy default_rng(INPUT_SEED + rank), uniform [0, 255])."""
+    return {"workload": f"u32 exclusive scan of n={args.n} elements, out of place, values uniform [0,255] from "
+                        f"numpy default_rng({INPUT_SEED} + rank)",
+            "n": args.n, "seed": INPUT_SEED, "parallelism": f"replicas x{world}",
+            "l2": "inputs and outputs of 1 GiB each exceed the 129 MB L2; no flush needed"}
+
+
+def workload_input(args, rank):
+    """The seeded input of one rank, on the host (uint32)."""
+    import numpy as np
+    return np.random.default_rng(INPUT_SEED + rank).integers(0, 256, size=args.n, dtype=np.uint32)
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -108,7 +128,10 @@ def profile_traffic_per_elem():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons, sampled every 100 ms."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms. The timed
+    region of a short run lasts milliseconds, so the window read back starts
+    with a soak of back-to-back untimed steps (about a second) just before it
+    and ends with it: the samples see the same load as the timed steps."""
     FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -125,11 +148,11 @@ class ClockSampler:
             os.close(fd)
             self.out = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                                          "-lms", "100", "-i", ident], stdout=self.out, stderr=subprocess.DEVNULL)
+                                          "-lms", "50", "-i", ident], stdout=self.out, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
-    def stop(self, t0, t1):
+    def stop(self, t_soak, t0, t1):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "note": "nvidia-smi unavailable"}
         time.sleep(0.25)
@@ -148,12 +171,15 @@ class ClockSampler:
                 except ValueError:
                     continue
         os.unlink(self.path)
-        window = [r for r in rows if t0 - 0.05 <= r[0] <= t1 + 0.05] or rows
+        window = [r for r in rows if t_soak <= r[0] <= t1 + 0.05]
         if not window:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "note": "no samples"}
         reasons = sorted({self.REASONS[i] for r in window for i, v in enumerate(r[3]) if v.lower() == "active"})
         return {"sm_mhz": statistics.median(r[1] for r in window), "sm_max_mhz": max(r[2] for r in window),
-                "reasons": reasons, "samples": len(window)}
+                "reasons": reasons, "samples": len(window),
+                "samples_in_timed_region": sum(1 for r in window if t0 - 0.05 <= r[0] <= t1 + 0.05),
+                "window_s": round(t1 - t_soak, 3),
+                "window": "soak of back-to-back untimed steps just before the timed region, then the timed region"}
 
 
 def max_over_ranks(value, dist=None, device="cuda"):
@@ -188,8 +214,7 @@ def run_reference(args, world, rank):
 
     import oracle
     threads = os.cpu_count() or 1
-    rng = np.random.default_rng(2028)
-    full = rng.integers(0, 256, size=args.n, dtype=np.uint32)
+    full = workload_input(args, rank)
     out = np.empty_like(full)
     t = time.perf_counter()
     oracle.scan_mt(full, out=out, inclusive=False, threads=threads)
@@ -211,8 +236,7 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "u32 exclusive scan of 2^28 elements, uniform [0,255], seeded",
-                   "n": args.n, "sample_elements_per_step": sample},
+        "config": workload_config(args, world),
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} of the {args.n} elements per step (3-phase reduce-then-scan "
                                    f"restated in oracle/scan_oracle.c, {threads} threads)"},
@@ -618,9 +642,9 @@ def run_ours(args, world, rank, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     n = args.n
     stream = torch.cuda.Stream()
-    gen = torch.Generator(device="cuda").manual_seed(2028 + rank)
+    h_in = torch.from_numpy(workload_input(args, rank).view(np.int32)).pin_memory()
     with torch.cuda.stream(stream):
-        d_in = torch.randint(0, 256, (n,), dtype=torch.int32, device="cuda", generator=gen)
+        d_in = h_in.to("cuda", non_blocking=True)
         d_out = torch.empty_like(d_in)
     stream.synchronize()
     plan = Plan(args.algo, "u32", max_n=n)
@@ -643,6 +667,13 @@ def run_ours(args, world, rank, local):
     stream.synchronize()
     sampler = ClockSampler(local)
     time.sleep(0.4)
+    # Clock soak: about a second of the same untimed steps, sampled together
+    # with the timed region that follows at once.
+    t_soak = time.time()
+    while time.time() - t_soak < args.clock_soak_s:
+        for _ in range(64):
+            step()
+        stream.synchronize()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -652,7 +683,7 @@ def run_ours(args, world, rank, local):
     t1 = time.time()
     if dist:
         dist.barrier()
-    clocks = sampler.stop(t0, t1)
+    clocks = sampler.stop(t_soak, t0, t1)
     plan.check(stream)
     ms = max_over_ranks(ms, dist)
     alg_bytes = n * 8
@@ -709,9 +740,7 @@ def run_ours(args, world, rank, local):
             compare["csdl_fallback_gbs"] = round(alg_bytes / (f_ms * 1e-3) / 1e9, 2)
 
         # End to end through the C ABI from pinned host memory.
-        h_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
         h_out = torch.empty(n, dtype=torch.int32, pin_memory=True)
-        h_in.copy_(d_in.cpu())
         plan.scan_host(h_in.data_ptr(), h_out.data_ptr(), n, stream=stream)
         if dist:
             dist.barrier()
@@ -755,9 +784,7 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"u32 exclusive scan, n={n}, {args.algo}, out of place, uniform [0,255] seeded",
-                   "n": n, "algo": args.algo, "parallelism": f"replicas x{world}",
-                   "l2": "inputs and outputs of 1 GiB each exceed the 129 MB L2; no flush needed"},
+        "config": workload_config(args, world), "algo": args.algo,
         "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 2) if kernel_gbs else None, "peak": peak,
                      "unit": "GB/s", "frac": round(kernel_gbs / peak, 4) if kernel_gbs else None,
                      "peak_kind": f"of {peak_kind}",

@@ -50,7 +50,10 @@ def common_flags() -> list[str]:
 
 
 def _newest_input_mtime() -> float:
-    files = glob.glob(os.path.join(CSRC_DIR, "*")) + glob.glob(os.path.join(INCLUDE_DIR, "*.h"))
+    """Newest source the library is built from: every file under csrc/ and
+    include/ (the kernels include include/gps_device.cuh), and this recipe."""
+    files = [f for d in (CSRC_DIR, INCLUDE_DIR) for f in glob.glob(os.path.join(d, "**", "*"), recursive=True)
+             if os.path.isfile(f)]
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
 

@@ -68,6 +68,34 @@ cudaError_t launch_l2_t(const ScanArgs& a, int num_sms, cudaStream_t stream, Lau
     return cudaGetLastError();
 }
 
+// Sets up (shared-memory opt-in, occupancy) the four kernels a chained scan
+// without forced stalls can launch: exclusive and inclusive, bulk-copy and
+// ring, without launching them.
+template <typename T>
+cudaError_t prepare_csdl_t() {
+    int occ = 0;
+    cudaError_t err = cudaSuccess;
+    {
+        constexpr size_t smem = l2_smem_bytes<T, kL2Warps, kL2RStages<T>, kL2SStages, kL2Queue, kL2Unit>();
+        constexpr int threads = L2Shape<T, kL2Warps>::kThreads;
+        err = resident_ctas_per_sm(scan_l2_kernel<T, kL2Warps, kL2RStages<T>, kL2SStages, kL2Queue, kL2Unit, false,
+                                                  false>, threads, smem, &occ);
+        if (err == cudaSuccess)
+            err = resident_ctas_per_sm(scan_l2_kernel<T, kL2Warps, kL2RStages<T>, kL2SStages, kL2Queue, kL2Unit, true,
+                                                      false>, threads, smem, &occ);
+    }
+    if (err == cudaSuccess) {
+        using Shape = TileShape<T, kCsdlWarps>;
+        constexpr size_t smem = pipeline_smem_bytes<T, kCsdlWarps, kCsdlStages>();
+        err = resident_ctas_per_sm(scan_pipeline_kernel<T, kCsdlWarps, kCsdlStages, kCsdlUnit, false, false,
+                                                        PrefixMode::Lookback, false>, Shape::kThreads, smem, &occ);
+        if (err == cudaSuccess)
+            err = resident_ctas_per_sm(scan_pipeline_kernel<T, kCsdlWarps, kCsdlStages, kCsdlUnit, true, false,
+                                                            PrefixMode::Lookback, false>, Shape::kThreads, smem, &occ);
+    }
+    return err;
+}
+
 template <typename T>
 cudaError_t dispatch_csdl(bool inclusive, bool stall, const ScanArgs& a, int num_sms, cudaStream_t stream,
                           LaunchInfo* info) {
@@ -92,6 +120,10 @@ uint32_t csdl_tile_elems(gps_dtype dtype) {
     // Struct elements (16 bytes) run on the generic kernel's 16 KB tiles.
     if (dtype == GPS_DTYPE_U32X4) return 16384 / 16;
     return dtype == GPS_DTYPE_U64 ? TileShape<uint64_t, kCsdlWarps>::kTile : TileShape<uint32_t, kCsdlWarps>::kTile;
+}
+
+cudaError_t prepare_csdl(gps_dtype dtype) {
+    return dtype == GPS_DTYPE_U64 ? prepare_csdl_t<uint64_t>() : prepare_csdl_t<uint32_t>();
 }
 
 cudaError_t launch_csdl(gps_dtype dtype, bool inclusive, bool stall_mode, const ScanArgs& a, int num_sms,

@@ -112,6 +112,9 @@ struct LaunchInfo {
 
 cudaError_t launch_csdl(gps_dtype dtype, bool inclusive, bool stall_mode, const ScanArgs& a,
                         int num_sms, cudaStream_t stream, LaunchInfo* info);
+// Sets up, without launching, every kernel launch_csdl() can pick for this
+// dtype without forced stalls, so that later launches make no set-up call.
+cudaError_t prepare_csdl(gps_dtype dtype);
 cudaError_t launch_rts(gps_dtype dtype, bool inclusive, const ScanArgs& a, void* tile_sums,
                        int num_sms, cudaStream_t stream, LaunchInfo* info);
 // Tensor maps of the generic kernel: the buffer seen as rows of 128 bytes

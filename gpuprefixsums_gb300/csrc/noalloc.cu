@@ -10,6 +10,7 @@
 // workspace header and the tile descriptors) in a fixed array of this file,
 // which the CUDA module holds on every device that loads the library, until
 // the process exits.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -17,6 +18,7 @@
 #include <mutex>
 
 #include "gps_internal.h"
+#include "launch_util.h"
 
 namespace {
 
@@ -38,9 +40,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 
+// Set-up of one device, valid for the driver context it was made in. The
+// device address of the array belongs to the context that loaded the module:
+// after cudaDeviceReset(), or when the caller makes another driver context
+// current on the same device, the array lives at another address. The
+// context's id (cuCtxGetId) is unique for the life of the process, so a
+// cached address is used only in the context that produced it.
 struct DeviceSetup {
-    bool ready;
-    void* scratch;  // device address of g_noalloc_scratch on this device
+    unsigned long long ctx_id;  // 0: not set up
+    void* scratch;              // device address of g_noalloc_scratch in that context
     int num_sms;
 };
 
@@ -80,17 +88,27 @@ gps_status gps_scan_u32_noalloc(gps_scan_kind kind, const void* d_in, void* d_ou
         return reject(GPS_ERR_CUDA, "gps_scan_u32_noalloc: no usable current device");
     DeviceSetup setup;
     {
-        // First call on this device: look up the scratch array's device
-        // address (and the SM count) with this device current.
+        // First call on this device in the current context: look up the
+        // scratch array's device address and the SM count with this device
+        // current, and set up the launch attributes of every kernel variant
+        // this entry point can launch, so that later calls (possibly inside a
+        // stream capture) query nothing.
         std::lock_guard<std::mutex> lock(g_setup_mu);
-        if (!g_setup[dev].ready) {
+        unsigned long long ctx = gps::current_ctx_id();
+        if (ctx == 0 || g_setup[dev].ctx_id != ctx) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr)
                 return reject(GPS_ERR_CUDA, "gps_scan_u32_noalloc: cudaGetSymbolAddress of the scratch array failed");
             int sms = 0;
             if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
                 return reject(GPS_ERR_CUDA, "gps_scan_u32_noalloc: device query failed");
-            g_setup[dev] = DeviceSetup{true, p, sms};
+            if (gps::prepare_csdl(GPS_DTYPE_U32) != cudaSuccess)
+                return reject(GPS_ERR_CUDA, "gps_scan_u32_noalloc: kernel set-up failed");
+            // cudaGetSymbolAddress has made the primary context current if no
+            // context was.
+            if (ctx == 0) ctx = gps::current_ctx_id();
+            if (ctx == 0) return reject(GPS_ERR_CUDA, "gps_scan_u32_noalloc: no current CUDA context");
+            g_setup[dev] = DeviceSetup{ctx, p, sms};
         }
         setup = g_setup[dev];
     }

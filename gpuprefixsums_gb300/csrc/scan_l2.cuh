@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(L2Shape<T, RW>::kThreads, 1) scan_l2_kernel(co
                     const uint32_t u = t / G;
                     const int q = static_cast<int>((rn / G) % Q);
                     bool publish = true;
-                    if (STALL && tile_is_stalled(a.stall, u)) {
+                    if (STALL && unit_stalls(a.stall, u, (a.num_tiles + G - 1) / G)) {
                         // Withhold the aggregate until the delay ends or a
                         // successor inserts it (EmulatedDeadlocking.cuh:64-70).
                         atomicAdd(&a.hdr->stat_stalls, 1ull);

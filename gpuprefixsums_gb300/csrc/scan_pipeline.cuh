@@ -141,6 +141,15 @@ __device__ __forceinline__ bool tile_is_stalled(const StallConfig& sc, uint32_t 
     return false;
 }
 
+// Whether lookback unit u of num_units withholds its aggregate. The last unit
+// never does: no successor exists to re-reduce it, so its stall would only
+// burn the delay (the reference's stalled tiles spin until a successor
+// rescues them, EmulatedDeadlocking.cuh:64-67, and it exempts a grid of one
+// tile; a stalled last tile there never returns).
+__device__ __forceinline__ bool unit_stalls(const StallConfig& sc, uint32_t u, uint32_t num_units) {
+    return u + 1 < num_units && tile_is_stalled(sc, u);
+}
+
 // Number of valid elements in tile t.
 template <int TILE>
 __device__ __forceinline__ uint32_t tile_count(uint64_t n, uint32_t t) {
@@ -733,7 +742,7 @@ __global__ void __launch_bounds__(TileShape<T, RW>::kThreads, 2) scan_pipeline_k
                         const uint32_t u = t / G;
                         word* desc = static_cast<word*>(a.desc);
                         bool publish = true;
-                        if (STALL && tile_is_stalled(a.stall, u)) {
+                        if (STALL && unit_stalls(a.stall, u, (a.num_tiles + G - 1) / G)) {
                             // Withhold the aggregate until the delay ends or a
                             // successor inserts it (EmulatedDeadlocking.cuh:64-70).
                             atomicAdd(&a.hdr->stat_stalls, 1ull);

@@ -272,13 +272,20 @@ gps_status gps_plan_geometry(gps_plan plan, uint64_t n, uint32_t* tile_elems, ui
  * GPS_NOALLOC_MAX_N returns GPS_ERR_SIZE_EXCEEDS_PLAN.
  *
  * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current, and sets up the kernels'
- * launch attributes; make that first call before any stream capture starts.
+ * (cudaGetSymbolAddress) with that device current, and sets up the launch
+ * attributes of all four kernels the call can launch (exclusive and
+ * inclusive, 16-byte-aligned and other buffers); make that first call before
+ * any stream capture starts. The set-up belongs to the CUDA context it was
+ * made in: after cudaDeviceReset(), or with another driver context current
+ * on the device, the next call makes it again, and that call too should come
+ * before any capture.
  * Every call clears the part of the array it uses with cudaMemsetAsync on
  * `stream`, because the array keeps what the previous call left. All calls
  * share the one array: two calls that can run at the same time on the GPU
  * (different streams, different host threads) race and give wrong results.
- * Device-side wait timeouts are not reported by this entry point. */
+ * Device-side waits are bounded (one second each) but this entry point has
+ * no plan to report a timeout through: a call whose wait ran out returns
+ * GPS_OK with an undefined output, and the next call clears the record. */
 gps_status gps_scan_u32_noalloc(gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
                                 gps_stream_t stream);
 

@@ -88,3 +88,31 @@ extern "C" int gps_devtest_run(int level, int op, int algo, const uint32_t* in, 
     }
     return -1;
 }
+
+namespace {
+// Holds its SM for `ns` nanoseconds of %globaltimer and exits: 1024 threads
+// and 227 KB of shared memory per CTA, so no other CTA fits beside it. Used
+// to run scans while part of the GPU is taken by another kernel. The wait is
+// bounded by the timer alone.
+__global__ void __launch_bounds__(1024, 1) occupy_kernel(unsigned long long ns) {
+    extern __shared__ unsigned char held[];
+    unsigned long long t0, now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    if (threadIdx.x == 0) held[0] = 1;
+    do {
+        __nanosleep(2000);
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    } while (now - t0 < ns);
+}
+}  // namespace
+
+// Launches `ctas` occupying CTAs for ns nanoseconds (at most 0.2 s) on
+// `stream`, without waiting for them. Returns the launch status.
+extern "C" int gps_devtest_occupy(unsigned ctas, unsigned long long ns, void* stream) {
+    constexpr int kSmem = 227 * 1024;
+    if (ns > 200000000ull) return -1;
+    cudaError_t err = cudaFuncSetAttribute(occupy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    if (err != cudaSuccess) return static_cast<int>(err);
+    occupy_kernel<<<ctas, 1024, kSmem, static_cast<cudaStream_t>(stream)>>>(ns);
+    return static_cast<int>(cudaGetLastError());
+}

@@ -75,6 +75,30 @@ class RefKernels:
         self._chk(self.cu.cuLaunchKernel(self.fn[key], grid, 1, 1, block, 1, 1, 0, ctypes.c_void_p(stream),
                                          params, None), f"launch {key}")
 
+    def csdl_device(self, buf, n: int, inclusive: bool, tbr=None, bump=None):
+        """The reference chained scan in place on the int32 device tensor
+        buf[:n], as DispatchKernels{Ex,In}clusive does
+        (ChainedScanDecoupledLookbackDispatcher.cuh:172-195): both memsets of
+        ClearMemory, then one launch. buf must hold at least align4(n)
+        elements (the kernel reads and writes up to there); tbr and bump are
+        reused when given. Asynchronous on the current stream."""
+        import torch
+        aligned = (n + 3) // 4 * 4
+        blocks = (aligned + PART - 1) // PART
+        if buf.numel() < aligned:
+            raise ValueError("buffer smaller than align4(n)")
+        if tbr is None or tbr.numel() < blocks:
+            tbr = torch.zeros(blocks, dtype=torch.int32, device=buf.device)
+        if bump is None:
+            bump = torch.zeros(1, dtype=torch.int32, device=buf.device)
+        tbr[:blocks].zero_()
+        bump.zero_()
+        stream = torch.cuda.current_stream().cuda_stream
+        key = "csdl_inclusive" if inclusive else "csdl_exclusive"
+        self._launch(key, blocks, 256, [Ptr(buf.data_ptr()), Ptr(tbr.data_ptr()), Ptr(bump.data_ptr()), aligned // 4],
+                     stream)
+        return buf
+
     def scan(self, algo: str, x: np.ndarray, inclusive: bool) -> np.ndarray:
         """Runs the reference kernel(s) in place on a padded copy of x (uint32)."""
         import torch

@@ -253,3 +253,87 @@ def test_fp32_sizes_and_segments(cuda, dt, inclusive):
             ex = oracle.scan_f32_exact(x[b:e], inclusive=inclusive)
             worst = max(worst, fp_errors(got[b:e], ex, x[b:e])[2])
     assert worst <= (1e-7 if dt == "f32c" else 1e-5), worst
+
+
+# ------------------------------------------------------ mixed batch (config 5)
+def zipf_lengths(count, s, lo, hi, seed):
+    """Continuous Zipf(s) truncated to [lo, hi], floored (inverse CDF)."""
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(0.0, 1.0, size=count)
+    a, b = lo ** (1.0 - s), hi ** (1.0 - s)
+    return np.clip(np.floor((a - u * (a - b)) ** (1.0 / (1.0 - s))), lo, hi).astype(np.int64)
+
+
+@pytest.mark.parametrize("inclusive", [False, True])
+def test_config5_mixed_batch_in_one_graph_against_the_oracle(cuda, inclusive):
+    # Config 5 at reduced size: 500 scans with Zipf(1.2) lengths in
+    # [32, 2^22], dtype per scan from {u32, u64, compensated f32}, batched per
+    # dtype, plus a 2^22-element u32 Bernoulli(0.3) flag scan; the four
+    # launches are captured in one CUDA graph and replayed twice.
+    count = 500
+    lengths = zipf_lengths(count, 1.2, 32, 2 ** 22, seed=50)
+    kinds = np.random.default_rng(51).integers(0, 3, size=count)
+    rng = np.random.default_rng(52)
+    groups = {}
+    for k, name in enumerate(("u32", "u64", "f32c")):
+        offs = offsets_of(lengths[kinds == k])
+        m = int(offs[-1])
+        if name == "u32":
+            x = rng.integers(0, 256, size=m, dtype=np.uint32)
+        elif name == "u64":
+            x = rng.integers(0, np.iinfo(np.uint64).max, size=m, dtype=np.uint64, endpoint=True)
+        else:
+            x = rng.standard_normal(m).astype(np.float32)
+        d_x = dev(x)
+        groups[name] = {"x": x, "offs": offs, "d_x": d_x, "out": torch.empty_like(d_x),
+                        "d_off": torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda(),
+                        "plan": Plan("csdl", name, max_n=m)}
+    nf = 1 << 22
+    flags = (rng.random(nf) < 0.3).astype(np.uint32)
+    d_flags, fout = dev(flags), torch.empty(nf, dtype=torch.int32, device="cuda")
+    fplan = Plan("csdl", "u32", max_n=nf)
+    st = torch.cuda.Stream()
+    try:
+        for g in groups.values():
+            g["plan"].autotune(g["d_x"], g["d_off"], out=g["out"], inclusive=inclusive, stream=st)
+
+        def batch():
+            for g in groups.values():
+                g["plan"].scan_segmented(g["d_x"], g["d_off"], out=g["out"], inclusive=inclusive, stream=st)
+            fplan.scan(d_flags, fout, inclusive=inclusive, stream=st)
+
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(st):
+            batch()
+            st.synchronize()
+            with torch.cuda.graph(graph, stream=st):
+                batch()
+        for _ in range(2):
+            for g in groups.values():
+                g["out"].fill_(-1)
+            fout.fill_(-1)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(st):
+                graph.replay()
+            st.synchronize()
+            for name in ("u32", "u64"):
+                g = groups[name]
+                got = g["out"].cpu().numpy().view(NP[name])
+                assert np.array_equal(got, oracle.segscan(g["x"], g["offs"], inclusive)), name
+            assert np.array_equal(fout.cpu().numpy().view(np.uint32), oracle.scan(flags, inclusive))
+            g = groups["f32c"]
+            got = g["out"].cpu().numpy()
+            worst_rel = worst_norm = 0.0
+            for s in range(len(g["offs"]) - 1):
+                b, e = int(g["offs"][s]), int(g["offs"][s + 1])
+                rel, _, norm = fp_errors(got[b:e], oracle.scan_f32_exact(g["x"][b:e], inclusive=inclusive),
+                                         g["x"][b:e])
+                worst_rel, worst_norm = max(worst_rel, rel), max(worst_norm, norm)
+            assert worst_rel <= 1e-6 and worst_norm <= 1e-7, (worst_rel, worst_norm)
+        for g in groups.values():
+            g["plan"].check(st)
+        fplan.check(st)
+    finally:
+        for g in groups.values():
+            g["plan"].close()
+        fplan.close()

@@ -29,3 +29,22 @@ def test_reference_arm_prints_one_contract_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert "workload" in line["config"]
+
+
+def test_both_arms_describe_the_same_workload():
+    # The GPU arm and the reference arm print the same config dict (n, seed,
+    # distribution) and draw the same seeded input.
+    import argparse
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    res = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n", str(1 << 20), "--steps", "1",
+                          "--warmup", "1"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    args = argparse.Namespace(n=1 << 20)
+    assert line["config"] == bench.workload_config(args, 1)
+    a, b = bench.workload_input(args, 0), bench.workload_input(args, 0)
+    assert a.dtype.name == "uint32" and (a == b).all() and int(a.max()) <= 255

@@ -86,8 +86,12 @@ def test_compat_selftest_was_built():
     assert os.access(SELFTEST_BIN, os.X_OK)
 
 
-REFERENCE_DRIVER = os.path.join(os.environ.get("GPS_REFERENCE_DIR", "/root/reference/GPUPrefixSumsCUDA"),
-                                "GPUPrefixSumsCUDA.cu")
+def _reference_driver():
+    from oracle.build import REFERENCE_SRC
+    return os.path.join(REFERENCE_SRC, "GPUPrefixSumsCUDA.cu")
+
+
+REFERENCE_DRIVER = _reference_driver()
 
 
 @pytest.mark.skipif(not os.path.exists(REFERENCE_DRIVER), reason="reference checkout not present")

@@ -441,3 +441,36 @@ def test_mid_max_takes_integer_chained_scan_plans_only(cuda):
             with pytest.raises(GpsError) as e:
                 plan.set_mid_max(1024)
             assert e.value.status == _lib.GPS_ERR_UNSUPPORTED
+
+
+def test_mid_size_scans_beside_a_kernel_holding_half_the_sms(cuda):
+    # The one-tile-per-CTA kernel takes tile ids from the block index when
+    # its grid fits the GPU at once; a CTA then waits only on lower block
+    # indices, which the hardware starts first. Here another stream's kernel
+    # holds half of the SMs (all of their shared memory) while mid-size scans
+    # run, so only part of each grid is resident at a time: the results stay
+    # exact and no wait runs out.
+    import ctypes
+
+    from gpuprefixsums_gb300 import build as B
+    dl = ctypes.CDLL(B.build_device_tests())
+    dl.gps_devtest_occupy.argtypes = [ctypes.c_uint, ctypes.c_ulonglong, ctypes.c_void_p]
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    side, main = torch.cuda.Stream(), torch.cuda.Stream()
+    sizes = [(1 << 20) - 5, 1 << 20, 600_001, 3 * 4096 * 40 + 7]
+    xs = [rand("u32", n, seed=n) for n in sizes]
+    d_in = [to_dev(x) for x in xs]
+    outs = [torch.empty_like(d) for d in d_in]
+    with Plan("csdl", "u32", max_n=1 << 20) as plan:
+        plan.set_small_max(0)
+        for _ in range(3):
+            torch.cuda.synchronize()
+            assert dl.gps_devtest_occupy(sms // 2, 30_000_000, ctypes.c_void_p(side.cuda_stream)) == 0
+            for d, o, n in zip(d_in, outs, sizes):
+                for inclusive in (False, True):
+                    plan.scan(d, o, inclusive=inclusive, n=n, stream=main)
+            main.synchronize()
+            plan.check(main)
+            for x, o in zip(xs, outs):
+                assert oracle.validate(x, to_host(o, np.uint32), True) == 0
+        side.synchronize()
