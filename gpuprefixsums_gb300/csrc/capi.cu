@@ -48,6 +48,9 @@ struct gps_plan_s {
     // u32 kernel; on other plans they are hdr and area.
     gps::WsHeader* hdr16;
     void* desc16;
+    // Integer chained-scan plans: the 16-byte, launch-tagged descriptors of
+    // the one-tile-per-CTA kernels (mid.cu), one per tile; else null.
+    void* desc_mid;
     // Integer scans of at most this many elements run in one CTA (small.cu).
     uint64_t small_max;
     uint64_t mid_max;  // chained-scan plans: largest scan run as one tile per CTA
@@ -153,6 +156,7 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     } else if (n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
         err = gps::launch_small(p->dtype, inclusive, a, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL && n <= p->mid_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
+        a.desc = p->desc_mid;
         err = gps::launch_mid(p->dtype, inclusive, a, p->num_sms, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
         err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0 || p->stall.fallback_polls != 0, a, p->num_sms,
@@ -234,11 +238,17 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     // use the generic kernel's 16-byte descriptors, kept in a region of their
     // own so that the two formats never meet in one slot.
     const uint64_t slots16 = (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? tiles + gps::kDescPad : 0;
-    // [header][carries][descriptors or tile sums] and, for u32 chained-scan
-    // plans, [256-byte aligned: generic header][16-byte descriptors].
+    // One-tile-per-CTA kernels of integer chained-scan plans: 16-byte
+    // descriptors tagged with the launch, in a region no other kernel uses.
+    const uint64_t slots_mid = (algo == GPS_ALGO_CSDL && !generic_only(dtype)) ? tiles + gps::kDescPad : 0;
+    // [header][carries][descriptors or tile sums]; for u32 chained-scan
+    // plans, [256-byte aligned: generic header][16-byte descriptors]; for
+    // integer chained-scan plans, [256-byte aligned: mid-size descriptors].
     const size_t main_bytes = kHeaderBytes + kCarryBytes + slots * per_tile;
     const size_t region16 = (main_bytes + 255) & ~static_cast<size_t>(255);
-    p->scratch_bytes = slots16 ? region16 + kHeaderBytes + slots16 * 16 : main_bytes;
+    const size_t end16 = slots16 ? region16 + kHeaderBytes + slots16 * 16 : main_bytes;
+    const size_t region_mid = (end16 + 255) & ~static_cast<size_t>(255);
+    p->scratch_bytes = slots_mid ? region_mid + slots_mid * 16 : end16;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;
@@ -250,6 +260,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
     p->hdr16 = slots16 ? reinterpret_cast<gps::WsHeader*>(static_cast<char*>(p->scratch) + region16) : p->hdr;
     p->desc16 = slots16 ? static_cast<char*>(p->scratch) + region16 + kHeaderBytes : p->area;
+    p->desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid : nullptr;
     gps::WsHeader h{};
     h.epoch = 1;
     h.capacity_tiles = slots;

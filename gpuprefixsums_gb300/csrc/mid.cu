@@ -2,27 +2,24 @@
 //
 // The persistent L2-buffered kernel (scan_l2.cuh) pays a pipeline latency of
 // about 10 us per launch (unit claim, HBM load, reduce, lookback, reload from
-// L2, scan, store), which dominates at small sizes. Here every tile
-// gets its own CTA of 256 threads and stays in registers between the two
-// halves of the scan, as in the reference's single-pass kernel
+// L2, scan, store), which dominates at small sizes. Here every tile gets its
+// own CTA of 256 threads, as in the reference's single-pass kernel
 // (ChainedScanDecoupledLookback.cuh:79-139):
-//   1. take a tile id: the block index when the whole grid is resident at
-//      once (every CTA it may wait on is running), else from the plan's
-//      atomic counter (ids follow the order in which CTAs start, so a CTA
-//      only waits on CTAs already running);
-//   2. load the tile (one bulk copy into shared memory for 16-byte-aligned
-//      buffers, else element by element); each thread sums its 64
-//      consecutive bytes (16 u32 or 8 u64) and the thread sums are
-//      block-scanned (include/gps_device.cuh);
-//   3. publish the tile aggregate, and let warp 0 walk back over the
-//      predecessors' descriptors (the same 8- or 16-byte descriptors, epoch
-//      and lookback as the L2 kernel: lookback() in scan_pipeline.cuh, here
-//      re-polling without back-off for the first polls: the predecessors'
-//      descriptors are typically microseconds away, not a unit's pipeline);
+//   1. the tile id is the block index: a CTA waits only on lower block
+//      indices, which the hardware dispatches first (CUB's decoupled
+//      lookback relies on the same order); every wait is bounded, so a
+//      violation would surface as GPS_ERR_TIMEOUT, never as a hang;
+//   2. load the tile and block-scan it;
+//   3. publish the tile aggregate, and let the whole CTA walk back over the
+//      predecessors' descriptors, 1024 of them per poll (block_lookback);
 //   4. publish the inclusive prefix, add the prefix, store.
-// The last CTA to be done with the descriptors resets the counters and
-// advances the epoch, as the L2 kernel does, so the two kernels share a
-// plan's scratch.
+// The kernels keep their descriptors in a region of the plan of their own,
+// tagged with the launch's grid id (%gridid: a 64-bit number the driver gives
+// every grid launched in a CUDA context, graph replays included). A
+// descriptor counts only when its tag is the current launch's, so a launch
+// needs neither a clearing memset nor an end-of-launch retirement (the last
+// CTA resetting counters and advancing an epoch): no atomic and no fence on
+// any CTA's path.
 #include "gps_device.cuh"
 #include "gps_internal.h"
 #include "launch_util.h"
@@ -32,52 +29,200 @@ namespace gps {
 namespace {
 
 constexpr int kMidThreads = 256;
+// Resident CTAs per SM the aligned-buffer kernel is compiled for.
+constexpr int kMidVecCtasPerSm = 8;
+// Descriptors each thread reads per lookback poll: a window of 1024 tiles.
+constexpr int kMidLookbackSlots = 4;
 
-// The last CTA to be done with the descriptors (its lookback finished and its
-// inclusive prefix published) returns the counters to zero and advances the
-// epoch, which retires every descriptor of this launch. Called by one thread
-// per CTA once its descriptor traffic is over; the output stores need no
-// ordering against it, so it runs while they drain.
-template <typename T>
-__device__ __forceinline__ void retire_launch(const ScanArgs& a, uint32_t epoch, bool block_ids) {
-    using D = DescTraits<T>;
-    __threadfence();
-    const uint32_t prev = atomicAdd(&a.hdr->exit_counter, 1u);
-    if (prev == gridDim.x - 1) {
-        __threadfence();
-        if (!block_ids) a.hdr->tile_counter = 0;
-        a.hdr->exit_counter = 0;
-        uint32_t e = epoch + 1;
-        if ((e & kEpochMask) == 0) {
-            typename D::word* desc = static_cast<typename D::word*>(a.desc);
-            for (unsigned long long q = 0; q < a.hdr->capacity_tiles; ++q) D::store(desc + q, D::zero());
-            e += 1;
-        }
-        __threadfence();
-        a.hdr->epoch = e;
+// ------------------------------------------------------------ descriptors
+// One 16-byte word per tile: {lo: the value (u32 or u64), hi: status:2 |
+// grid id:62}. Zeroed memory reads "not ready". 2^62 launches would have to
+// pass in one context before a stale tag could come round again.
+constexpr uint64_t kGidMask = (1ull << 62) - 1;
+
+struct MidDesc {
+    __device__ static ptx::u64x2 pack(uint32_t status, uint64_t gid, uint64_t v) {
+        ptx::u64x2 w;
+        w.lo = v;
+        w.hi = (static_cast<uint64_t>(status) << 62) | (gid & kGidMask);
+        return w;
     }
+    __device__ static uint32_t status(const ptx::u64x2& w, uint64_t gid) {
+        return (w.hi & kGidMask) == (gid & kGidMask) ? static_cast<uint32_t>(w.hi >> 62) : kNotReady;
+    }
+};
+
+__device__ __forceinline__ uint64_t grid_id() {
+    uint64_t g;
+    asm volatile("mov.u64 %0, %%gridid;" : "=l"(g));
+    return g;
+}
+
+// ---------------------------------------------------------- block lookback
+// Shared memory of block_lookback: two rounds of per-warp results.
+template <typename T, int THREADS>
+struct LookbackSmem {
+    uint32_t incl_pos[THREADS / 32];
+    uint32_t gap_pos[THREADS / 32];
+    T part[THREADS / 32];
+    uint32_t give_up;
+};
+
+// Exclusive prefix of tile t > 0 (sum of tiles 0 .. t-1), computed by every
+// thread of the CTA together and returned to all of them. Each poll reads a
+// window of SLOTS * THREADS descriptors below t -- thread i the slots at
+// positions i, i + THREADS, ... (position p is slot t - 1 - p, so a warp's
+// loads are 512 contiguous bytes) -- and needs two barrier rounds: the
+// nearest inclusive prefix, then the nearest slot still not ready below it
+// and the sum of the values up to it. A window of aggregates only moves the
+// walk back by a whole window; a window with a slot not ready is polled again
+// (only the slots not ready are re-read), with back-off after SPIN polls and
+// the plan's wait budget as the bound. Tile 0 publishes an inclusive prefix,
+// so every walk ends there at the latest. The descriptors of a 2^22-element
+// u32 scan (1024 tiles) fit in one window.
+template <typename T, int THREADS, int SLOTS, uint32_t SPIN = 64>
+__device__ T block_lookback(const ScanArgs& a, const ptx::u64x2* desc, uint32_t t, uint64_t gid,
+                            LookbackSmem<T, THREADS>& sm) {
+    constexpr int WARPS = THREADS / 32;
+    constexpr uint32_t WIN = static_cast<uint32_t>(THREADS * SLOTS);
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31u;
+    const uint32_t warp = tid >> 5;
+    T prefix = 0;
+    int64_t top = static_cast<int64_t>(t) - 1;  // slot at position 0
+    uint32_t polls = 0;
+    uint64_t deadline = 0;
+    uint32_t backoff = 32;
+    while (true) {
+        T val[SLOTS];
+        uint32_t valid = 0, incl = 0, pending = 0;
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j) {
+            val[j] = 0;
+            if (top - static_cast<int64_t>(tid + j * THREADS) < 0)
+                valid |= 1u << j;  // below slot 0: never summed (slot 0 is inclusive)
+            else
+                pending |= 1u << j;
+        }
+        while (true) {
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j) {
+                if ((pending >> j) & 1u) {
+                    const ptx::u64x2 w = ptx::ld_relaxed_b128(desc + (top - static_cast<int64_t>(tid + j * THREADS)));
+                    const uint32_t st = MidDesc::status(w, gid);
+                    if (st != kNotReady) {
+                        valid |= 1u << j;
+                        pending &= ~(1u << j);
+                        val[j] = static_cast<T>(w.lo);
+                        if (st == kInclusive) incl |= 1u << j;
+                    }
+                }
+            }
+            // Round 1: the nearest inclusive prefix.
+            uint32_t my = kNone;
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+                if ((incl >> j) & 1u) my = min(my, tid + j * THREADS);
+            my = __reduce_min_sync(kFullMask, my);
+            if (lane == 0) sm.incl_pos[warp] = my;
+            __syncthreads();
+            uint32_t pinc = kNone;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) pinc = min(pinc, sm.incl_pos[w]);
+            // Round 2: the nearest slot not ready below it, and the sum up to it.
+            uint32_t gap = kNone;
+            T part = 0;
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j) {
+                const uint32_t pos = tid + j * THREADS;
+                if (pos <= pinc) {
+                    if ((valid >> j) & 1u)
+                        part += val[j];
+                    else
+                        gap = min(gap, pos);
+                }
+            }
+            gap = __reduce_min_sync(kFullMask, gap);
+            part = warp_sum(part);
+            if (lane == 0) {
+                sm.gap_pos[warp] = gap;
+                sm.part[warp] = part;
+            }
+            if (tid == 0) {
+                bool give_up = false;
+                if ((polls & 15u) == 1u) {
+                    const uint64_t now = ptx::global_timer_ns();
+                    if (deadline == 0) deadline = now + a.wait_budget_ns;
+                    give_up = now > deadline || ld_volatile_u32(&a.hdr->error_flags) != 0;
+                }
+                sm.give_up = give_up;
+            }
+            __syncthreads();
+            gap = kNone;
+            part = 0;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) {
+                gap = min(gap, sm.gap_pos[w]);
+                part += sm.part[w];
+            }
+            if (gap == kNone) {
+                prefix += part;
+                if (pinc != kNone) return prefix;
+                top -= WIN;  // a window of aggregates only
+                polls = 0;
+                break;
+            }
+            if (sm.give_up) {
+                if (tid == 0) raise_error(a.hdr, kErrLookbackTimeout);
+                return prefix;
+            }
+            ++polls;
+            if (polls > SPIN) {
+                __nanosleep(backoff);
+                backoff = backoff < 1024 ? backoff * 2 : 1024;
+            }
+        }
+    }
+}
+
+// Publishes tile t's aggregate, resolves its exclusive prefix (carry_in for
+// tile 0) and publishes its inclusive prefix; returns the prefix to every
+// thread. `total` is the tile's sum, known to every thread.
+template <typename T>
+__device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint64_t gid, T total,
+                                             LookbackSmem<T, kMidThreads>& sm) {
+    ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
+    const T carry = a.carry_in != nullptr ? *static_cast<const T*>(a.carry_in) : T(0);
+    if (t == 0) {
+        if (threadIdx.x == 0) {
+            ptx::st_relaxed_b128(desc, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(carry + total)));
+            if (a.carry_out != nullptr && a.num_tiles == 1) *static_cast<T*>(a.carry_out) = carry + total;
+        }
+        return carry;
+    }
+    if (threadIdx.x == 0) ptx::st_relaxed_b128(desc + t, MidDesc::pack(kAggregate, gid, static_cast<uint64_t>(total)));
+    // Tile 0's inclusive prefix holds the carry, so the lookback's sum does too.
+    const T pre = block_lookback<T, kMidThreads, kMidLookbackSlots>(a, desc, t, gid, sm);
+    if (threadIdx.x == 0) {
+        ptx::st_relaxed_b128(desc + t, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
+        if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
+    }
+    return pre;
 }
 
 // Buffers not aligned to 16 bytes: each thread loads and stores its 64
 // bytes element by element.
 template <typename T, bool INCL>
-__global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs a, bool block_ids) {
+__global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs a) {
     constexpr int TILE = 16384 / static_cast<int>(sizeof(T));
     constexpr int ITEMS = TILE / kMidThreads;  // 16 u32 or 8 u64: 64 bytes
-    using D = DescTraits<T>;
-    using word = typename D::word;
     __shared__ gps_device::BlockScanStorage<kMidThreads, T> st;
-    __shared__ uint32_t s_tile;
-    __shared__ T s_prefix;
+    __shared__ LookbackSmem<T, kMidThreads> lsm;
 
     const uint32_t tid = threadIdx.x;
-    const uint32_t lane = tid & 31u;
-    if (!block_ids) {
-        if (tid == 0) s_tile = atomicAdd(&a.hdr->tile_counter, 1u);
-        __syncthreads();
-    }
-    const uint32_t t = block_ids ? blockIdx.x : s_tile;
-    const uint32_t epoch = ld_volatile_u32(&a.hdr->epoch);
+    const uint32_t t = blockIdx.x;
+    const uint64_t gid = grid_id();
     const T* in = static_cast<const T*>(a.in);
     T* out = static_cast<T*>(a.out);
     const uint64_t i0 = static_cast<uint64_t>(t) * TILE + static_cast<uint64_t>(tid) * ITEMS;
@@ -90,22 +235,7 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
     for (int e = 0; e < ITEMS; ++e) sum += v[e];
     T total;
     const T before = gps_device::block_exclusive_scan<kMidThreads>(sum, st, gps_device::Plus(), &total);
-
-    word* desc = static_cast<word*>(a.desc);
-    const T carry = a.carry_in != nullptr ? *static_cast<const T*>(a.carry_in) : T(0);
-    if (tid < 32) {
-        if (lane == 0)
-            D::store(desc + t, t == 0 ? D::pack(kInclusive, epoch, carry + total) : D::pack(kAggregate, epoch, total));
-        const T pre = t == 0 ? carry : lookback<T, TILE, false, 64>(a, t, epoch, lane, carry, -1, T(0));
-        if (lane == 0) {
-            if (t != 0) D::store(desc + t, D::pack(kInclusive, epoch, pre + total));
-            if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
-            s_prefix = pre;
-        }
-    }
-    __syncthreads();
-
-    T run = s_prefix + before;
+    T run = mid_tile_prefix<T>(a, t, gid, total, lsm) + before;
 #pragma unroll
     for (int e = 0; e < ITEMS; ++e) {
         const T x = v[e];
@@ -120,155 +250,147 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
 #pragma unroll
     for (int e = 0; e < ITEMS; ++e)
         if (i0 + e < a.n) out[i0 + e] = v[e];
-    if (tid == 0) retire_launch<T>(a, epoch, block_ids);
 }
 
-// The same scan for 16-byte-aligned buffers, with the tile moved by one bulk
-// copy each way (cp.async.bulk into and out of shared memory) instead of
-// strided per-thread accesses. Each thread reads its four 16-byte chunks in
-// an order rotated by (tid >> 1) & 3, which spreads every quarter-warp over
-// all 32 banks; rotated_chunk_prefix() undoes the rotation arithmetically.
+// The same scan for 16-byte-aligned buffers. The tile is four rows of 256
+// 16-byte chunks, and thread tid holds chunk tid of every row, so each warp
+// load or store instruction covers 512 contiguous bytes. The exclusive prefix
+// of chunk (r, tid) within the tile is the sum of the rows before r plus the
+// chunks of row r before tid: the four chunk sums are warp-scanned together,
+// the warp totals go through shared memory in row-major order (row r, warp
+// w at r * 8 + w), and one warp scan of those 32 totals gives every (row,
+// warp) its offset -- one barrier for the whole block scan. Chunks are read
+// twice: for the sums, and after the lookback to scan and store them (the
+// second read hits this SM's L1). Neither tile data nor chunk offsets stay in
+// registers across the lookback, which keeps the kernel at 32 registers and
+// eight CTAs per SM: on 152 SMs up to 1216 tiles (2^22 u32 elements fit) run
+// in one wave. There is no shared-memory staging and no mbarrier to set up,
+// so every CTA issues its loads as soon as it starts.
 template <typename T, bool INCL>
-__global__ void __launch_bounds__(kMidThreads, 2) mid_bulk_kernel(const ScanArgs a, bool block_ids) {
+__global__ void __launch_bounds__(kMidThreads, kMidVecCtasPerSm) mid_vec_kernel(const ScanArgs a) {
     constexpr int TILE = 16384 / static_cast<int>(sizeof(T));
-    constexpr int ITEMS = TILE / kMidThreads;
     constexpr int EPC = 16 / static_cast<int>(sizeof(T));
-    constexpr int CHUNKS = ITEMS / EPC;  // 4
-    using D = DescTraits<T>;
-    using word = typename D::word;
-    __shared__ __align__(128) T tile[TILE];
-    __shared__ uint64_t bar;
-    __shared__ gps_device::BlockScanStorage<kMidThreads, T> st;
-    __shared__ uint32_t s_tile;
-    __shared__ T s_prefix;
+    constexpr int ROW = kMidThreads * EPC;  // elements per row
+    constexpr int ROWS = TILE / ROW;        // 4
+    constexpr int WARPS = kMidThreads / 32;
+    static_assert(ROWS * WARPS == 32, "one warp scans all (row, warp) totals");
+    __shared__ T s_tot[ROWS * WARPS];
+    __shared__ T s_off[ROWS][kMidThreads];  // chunk offsets, kept here across the lookback
+    __shared__ LookbackSmem<T, kMidThreads> lsm;
 
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31u;
-    if (tid == 0) {
-        if (!block_ids) s_tile = atomicAdd(&a.hdr->tile_counter, 1u);
-        ptx::mbar_init(&bar, 1);
-        ptx::fence_mbar_init();
-    }
-    __syncthreads();
-    const uint32_t t = block_ids ? blockIdx.x : s_tile;
-    const uint32_t epoch = ld_volatile_u32(&a.hdr->epoch);
+    const uint32_t warp = tid >> 5;
+    const uint32_t t = blockIdx.x;
+    const uint64_t gid = grid_id();
     const uint64_t t0 = static_cast<uint64_t>(t) * TILE;
+    // Elements of this tile; chunk (r, tid) starts at element r * ROW + tid * EPC.
     const uint32_t cnt = static_cast<uint32_t>(min(static_cast<uint64_t>(TILE), a.n - t0));
-    const uint32_t bulk = (cnt * static_cast<uint32_t>(sizeof(T))) & ~15u;
-    const uint32_t bulk_elems = bulk / static_cast<uint32_t>(sizeof(T));
-    const T* in = static_cast<const T*>(a.in);
-    T* out = static_cast<T*>(a.out);
-    if (tid == 0) {
-        ptx::mbar_arrive_expect_tx(&bar, bulk);
-        if (bulk) ptx::bulk_load(tile, in + t0, bulk, &bar);
-    }
-    // The ragged end of the last tile (under 16 bytes) by plain loads.
-    if (tid < cnt - bulk_elems) tile[bulk_elems + tid] = in[t0 + bulk_elems + tid];
-    const bool landed =
-        ptx::mbar_try_wait(&bar, 0) || ptx::mbar_wait_bounded(&bar, 0, ptx::global_timer_ns() + a.wait_budget_ns);
-    if (!landed) raise_error(a.hdr, kErrPipelineTimeout);
-    __syncthreads();
+    const bool full = cnt == static_cast<uint32_t>(TILE);
+    const T* src = static_cast<const T*>(a.in) + t0 + tid * EPC;
+    T* dst = static_cast<T*>(a.out) + t0 + tid * EPC;
 
-    const uint32_t rot = (tid >> 1) & (CHUNKS - 1);
-    const bool whole = (tid + 1) * ITEMS <= cnt;
-    T v[ITEMS];
-    T cs[CHUNKS];
+    T cs[ROWS];
+    {
+        Chunk<T> q[ROWS];
 #pragma unroll
-    for (int c8 = 0; c8 < CHUNKS; ++c8) {
-        const uint32_t c = (c8 + rot) & (CHUNKS - 1);
-        const Chunk<T> q = *reinterpret_cast<const Chunk<T>*>(tile + tid * ITEMS + c * EPC);
-        T x = 0;
+        for (int r = 0; r < ROWS; ++r) {
+            const uint32_t off = r * ROW + tid * EPC;
+            if (full || off + EPC <= cnt) {
+                q[r] = *reinterpret_cast<const Chunk<T>*>(src + r * ROW);
+            } else {
 #pragma unroll
-        for (int e = 0; e < EPC; ++e) {
-            const T y = (whole || tid * ITEMS + c * EPC + e < cnt) ? q.v[e] : T(0);
-            v[c8 * EPC + e] = y;
-            x += y;
+                for (int e = 0; e < EPC; ++e) q[r].v[e] = off + e < cnt ? src[r * ROW + e] : T(0);
+            }
         }
-        cs[c8] = x;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            T x = 0;
+#pragma unroll
+            for (int e = 0; e < EPC; ++e) x += q[r].v[e];
+            cs[r] = x;
+        }
     }
-    T cpre[CHUNKS];
-    T sum;
-    rotated_chunk_prefix<T, CHUNKS>(cs, rot, cpre, sum);
+    // Block scan of the four rows at once; each thread's four chunk offsets
+    // wait in shared memory during the lookback.
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        T wt;
+        cs[r] = gps_device::warp_exclusive_scan<gps_device::WarpAlgo::KoggeStone>(cs[r], gps_device::Plus(), &wt);
+        if (lane == 0) s_tot[r * WARPS + warp] = wt;
+    }
+    __syncthreads();
     T total;
-    const T before = gps_device::block_exclusive_scan<kMidThreads>(sum, st, gps_device::Plus(), &total);
+    {
+        const T x = s_tot[lane];
+        const T xi = gps_device::warp_inclusive_scan<gps_device::WarpAlgo::KoggeStone>(x, gps_device::Plus());
+        const T xe = xi - x;
+        total = __shfl_sync(kFullMask, xi, 31);
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) s_off[r][tid] = cs[r] + __shfl_sync(kFullMask, xe, r * WARPS + warp);
+    }
 
-    word* desc = static_cast<word*>(a.desc);
-    const T carry = a.carry_in != nullptr ? *static_cast<const T*>(a.carry_in) : T(0);
-    if (tid < 32) {
-        if (lane == 0)
-            D::store(desc + t, t == 0 ? D::pack(kInclusive, epoch, carry + total) : D::pack(kAggregate, epoch, total));
-        const T pre = t == 0 ? carry : lookback<T, TILE, false, 64>(a, t, epoch, lane, carry, -1, T(0));
-        if (lane == 0) {
-            if (t != 0) D::store(desc + t, D::pack(kInclusive, epoch, pre + total));
-            if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
-            s_prefix = pre;
+    const T base = mid_tile_prefix<T>(a, t, gid, total, lsm);
+
+    Chunk<T> q[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const uint32_t off = r * ROW + tid * EPC;
+        if (full || off + EPC <= cnt) {
+            q[r] = *reinterpret_cast<const Chunk<T>*>(src + r * ROW);
+        } else {
+#pragma unroll
+            for (int e = 0; e < EPC; ++e) q[r].v[e] = off + e < cnt ? src[r * ROW + e] : T(0);
         }
     }
-    __syncthreads();
-
-    const T base = s_prefix + before;
 #pragma unroll
-    for (int c8 = 0; c8 < CHUNKS; ++c8) {
-        T acc = base + cpre[c8];
-        Chunk<T> q;
+    for (int r = 0; r < ROWS; ++r) {
+        const uint32_t off = r * ROW + tid * EPC;
+        T acc = base + s_off[r][tid];
 #pragma unroll
         for (int e = 0; e < EPC; ++e) {
-            const T x = v[c8 * EPC + e];
+            const T x = q[r].v[e];
             if (INCL) {
                 acc += x;
-                q.v[e] = acc;
+                q[r].v[e] = acc;
             } else {
-                q.v[e] = acc;
+                q[r].v[e] = acc;
                 acc += x;
             }
         }
-        const uint32_t c = (c8 + rot) & (CHUNKS - 1);
-        *reinterpret_cast<Chunk<T>*>(tile + tid * ITEMS + c * EPC) = q;
-    }
-    ptx::fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0 && bulk) {
-        ptx::bulk_store(out + t0, tile, bulk);
-        ptx::bulk_commit();
-    }
-    if (tid < cnt - bulk_elems) out[t0 + bulk_elems + tid] = tile[bulk_elems + tid];
-    if (tid == 0) {
-        retire_launch<T>(a, epoch, block_ids);
-        // The store must have read the tile before the CTA's shared memory
-        // goes away.
-        if (bulk) ptx::bulk_wait_read<0>();
+        if (full || off + EPC <= cnt) {
+            *reinterpret_cast<Chunk<T>*>(dst + r * ROW) = q[r];
+        } else {
+#pragma unroll
+            for (int e = 0; e < EPC; ++e)
+                if (off + e < cnt) dst[r * ROW + e] = q[r].v[e];
+        }
     }
 }
 
 template <typename T, bool INCL, bool VEC>
-cudaError_t launch_mid_v(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
-    auto kern = VEC ? mid_bulk_kernel<T, INCL> : mid_scan_kernel<T, INCL>;
-    int occ = 0;
-    cudaError_t err = resident_ctas_per_sm(kern, kMidThreads, 0, &occ);
-    if (err != cudaSuccess) return err;
+cudaError_t launch_mid_v(const ScanArgs& a, cudaStream_t stream, LaunchInfo* info) {
+    auto kern = VEC ? mid_vec_kernel<T, INCL> : mid_scan_kernel<T, INCL>;
     const int grid = static_cast<int>(a.num_tiles);
-    const bool block_ids = static_cast<int64_t>(grid) <= static_cast<int64_t>(occ) * num_sms;
     if (info) *info = LaunchInfo{grid, kMidThreads, 0};
-    kern<<<grid, kMidThreads, 0, stream>>>(a, block_ids);
+    kern<<<grid, kMidThreads, 0, stream>>>(a);
     return cudaGetLastError();
 }
 
 template <typename T, bool INCL>
-cudaError_t launch_mid_t(const ScanArgs& a, int num_sms, cudaStream_t stream, LaunchInfo* info) {
+cudaError_t launch_mid_t(const ScanArgs& a, cudaStream_t stream, LaunchInfo* info) {
+    if ((reinterpret_cast<uintptr_t>(a.desc) & 15u) != 0) return cudaErrorInvalidValue;
     const bool vec = ((reinterpret_cast<uintptr_t>(a.in) | reinterpret_cast<uintptr_t>(a.out)) & 15u) == 0;
-    return vec ? launch_mid_v<T, INCL, true>(a, num_sms, stream, info)
-               : launch_mid_v<T, INCL, false>(a, num_sms, stream, info);
+    return vec ? launch_mid_v<T, INCL, true>(a, stream, info) : launch_mid_v<T, INCL, false>(a, stream, info);
 }
 
 }  // namespace
 
-cudaError_t launch_mid(gps_dtype dtype, bool inclusive, const ScanArgs& a, int num_sms, cudaStream_t stream,
+cudaError_t launch_mid(gps_dtype dtype, bool inclusive, const ScanArgs& a, int /*num_sms*/, cudaStream_t stream,
                        LaunchInfo* info) {
     if (dtype == GPS_DTYPE_U64)
-        return inclusive ? launch_mid_t<uint64_t, true>(a, num_sms, stream, info)
-                         : launch_mid_t<uint64_t, false>(a, num_sms, stream, info);
-    return inclusive ? launch_mid_t<uint32_t, true>(a, num_sms, stream, info)
-                     : launch_mid_t<uint32_t, false>(a, num_sms, stream, info);
+        return inclusive ? launch_mid_t<uint64_t, true>(a, stream, info) : launch_mid_t<uint64_t, false>(a, stream, info);
+    return inclusive ? launch_mid_t<uint32_t, true>(a, stream, info) : launch_mid_t<uint32_t, false>(a, stream, info);
 }
 
 }  // namespace gps

@@ -175,9 +175,9 @@ __device__ T warp_reduce_tile_input(const T* in, uint64_t n, uint32_t t, uint32_
 // Descriptors read by each lane per poll: 128 bytes, i.e. 16 u32-scan
 // descriptors or 8 u64-scan descriptors; a window is 32 lanes of that (512 or
 // 256 slots).
-template <typename W>
+template <typename W, int LANE_BYTES = 128>
 constexpr int lookback_per_lane() {
-    return 128 / static_cast<int>(sizeof(W));
+    return LANE_BYTES / static_cast<int>(sizeof(W));
 }
 
 // Run by one whole warp for lookback unit u > 0 (a tile, or a group of SPAN
@@ -194,12 +194,16 @@ constexpr int lookback_per_lane() {
 // slot not ready re-reads only the pairs holding such slots, after an
 // exponential back-off (from poll SPIN on; the polls before it re-read at
 // once). Bounded by the wait budget.
-template <typename T, int SPAN, bool STALL, uint32_t SPIN = 0>
+// LANE_BYTES (16 to 128) sets the descriptor bytes each lane reads per poll,
+// and so the window: kernels short of registers read narrower windows.
+template <typename T, int SPAN, bool STALL, uint32_t SPIN = 0, int LANE_BYTES = 128>
 __device__ T lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane, T carry, int64_t bound,
                       T bound_val) {
     using D = DescTraits<T>;
     using word = typename D::word;
-    constexpr int K = lookback_per_lane<word>();        // slots per lane
+    static_assert(LANE_BYTES >= 16 && LANE_BYTES <= 128 && (LANE_BYTES & (LANE_BYTES - 1)) == 0,
+                  "16 to 128 bytes per lane, a power of two");
+    constexpr int K = lookback_per_lane<word, LANE_BYTES>();  // slots per lane
     constexpr int PAIR = 16 / static_cast<int>(sizeof(word));  // slots per 16-byte access
     constexpr int NACC = K / PAIR;                      // accesses per lane
     constexpr int WIN = 32 * K;                         // slots per window
