@@ -51,6 +51,7 @@ struct gps_plan_s {
     // Integer chained-scan plans: the 16-byte, launch-tagged descriptors of
     // the one-tile-per-CTA kernels (mid.cu), one per tile; else null.
     void* desc_mid;
+    void* group_desc_mid;  // and one per group of 32 tiles
     // Integer scans of at most this many elements run in one CTA (small.cu).
     uint64_t small_max;
     uint64_t mid_max;  // chained-scan plans: largest scan run as one tile per CTA
@@ -157,6 +158,7 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
         err = gps::launch_small(p->dtype, inclusive, a, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL && n <= p->mid_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
         a.desc = p->desc_mid;
+        a.group_desc = p->group_desc_mid;
         err = gps::launch_mid(p->dtype, inclusive, a, p->num_sms, stream, &p->last_launch);
     } else if (p->algo == GPS_ALGO_CSDL) {
         err = gps::launch_csdl(p->dtype, inclusive, p->stall.mode != 0 || p->stall.fallback_polls != 0, a, p->num_sms,
@@ -222,7 +224,12 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->capacity_tiles = tiles;
     p->wait_budget_ns = kDefaultBudgetNs;
     std::memset(p->tuned, -1, sizeof(p->tuned));
-    p->small_max = gps::small_scan_max_elems(dtype);
+    // Chained-scan plans send small integer scans to the one-tile-per-CTA
+    // kernel too: measured on GB300 it matches or beats the one-CTA kernel
+    // at every size up to 64 KB (2.0 against 2.2-2.35 us up to one tile,
+    // 2.7 against 4.5 us at 16384 u32). Reduce-then-scan plans keep the
+    // one-CTA kernel for small inputs.
+    p->small_max = algo == GPS_ALGO_CSDL ? 0 : gps::small_scan_max_elems(dtype);
     p->mid_max = algo == GPS_ALGO_CSDL && !generic_only(dtype) ? gps::kMidMaxBytes / gps::dtype_size(dtype) : 0;
     cudaError_t err = cudaGetDevice(&p->device);
     if (err == cudaSuccess) err = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
@@ -241,6 +248,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     // One-tile-per-CTA kernels of integer chained-scan plans: 16-byte
     // descriptors tagged with the launch, in a region no other kernel uses.
     const uint64_t slots_mid = (algo == GPS_ALGO_CSDL && !generic_only(dtype)) ? tiles + gps::kDescPad : 0;
+    const uint64_t groups_mid = slots_mid ? (tiles + 31) / 32 + gps::kDescPad : 0;
     // [header][carries][descriptors or tile sums]; for u32 chained-scan
     // plans, [256-byte aligned: generic header][16-byte descriptors]; for
     // integer chained-scan plans, [256-byte aligned: mid-size descriptors].
@@ -248,7 +256,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     const size_t region16 = (main_bytes + 255) & ~static_cast<size_t>(255);
     const size_t end16 = slots16 ? region16 + kHeaderBytes + slots16 * 16 : main_bytes;
     const size_t region_mid = (end16 + 255) & ~static_cast<size_t>(255);
-    p->scratch_bytes = slots_mid ? region_mid + slots_mid * 16 : end16;
+    p->scratch_bytes = slots_mid ? region_mid + (slots_mid + groups_mid) * 16 : end16;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;
@@ -261,6 +269,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->hdr16 = slots16 ? reinterpret_cast<gps::WsHeader*>(static_cast<char*>(p->scratch) + region16) : p->hdr;
     p->desc16 = slots16 ? static_cast<char*>(p->scratch) + region16 + kHeaderBytes : p->area;
     p->desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid : nullptr;
+    p->group_desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid + slots_mid * 16 : nullptr;
     gps::WsHeader h{};
     h.epoch = 1;
     h.capacity_tiles = slots;

@@ -76,6 +76,7 @@ struct ScanArgs {
     uint32_t pad_;
     WsHeader* hdr;       // plan state (counters, epoch, error flags)
     void* desc;          // tile descriptors (lookback)
+    void* group_desc;    // one-tile-per-CTA kernels: descriptors of groups of 32 tiles
     const void* spine;   // inclusive scan of tile sums (reduce-then-scan)
     const void* carry_in;  // optional: one element added to every output
     void* carry_out;       // optional: receives carry_in + sum of all n inputs
@@ -165,11 +166,13 @@ constexpr size_t kSmallMaxBytes = 64 * 1024;
 uint64_t small_scan_max_elems(gps_dtype dtype);
 cudaError_t launch_small(gps_dtype dtype, bool inclusive, const ScanArgs& a, cudaStream_t stream, LaunchInfo* info);
 
-// Mid-size integer chained scans, one 16 KB tile per CTA (mid.cu); the
-// default upper size of a plan, in bytes of input (measured on GB300: one
-// tile per CTA is faster than the persistent kernel up to 2^20 u32, 7.7
-// against 10.4 us, and slower from 2^21 on, 15.0 against 12.1 us).
-constexpr size_t kMidMaxBytes = 4ull << 20;
+// Integer chained scans up to mid size, one 16 KB tile per CTA (mid.cu); the
+// default upper size of a plan, in bytes of input. Measured on GB300 (graph
+// replay, L2-resident buffers): one tile per CTA is faster than the
+// persistent kernel up to 48 MB (u32: 13.0 against 16.5 us at 3 x 2^22;
+// u64: 25.4 against 26.8 us at 3 x 2^21), slower at 64 MB (u32: 37.4 against
+// 34.6 us at 2^24; u64: 38.4 against 32.7 us at 2^23).
+constexpr size_t kMidMaxBytes = 48ull << 20;
 cudaError_t launch_mid(gps_dtype dtype, bool inclusive, const ScanArgs& a, int num_sms, cudaStream_t stream,
                        LaunchInfo* info);
 

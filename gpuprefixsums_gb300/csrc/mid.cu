@@ -10,8 +10,9 @@
 //      lookback relies on the same order); every wait is bounded, so a
 //      violation would surface as GPS_ERR_TIMEOUT, never as a hang;
 //   2. load the tile and block-scan it;
-//   3. publish the tile aggregate, and let the whole CTA walk back over the
-//      predecessors' descriptors, 1024 of them per poll (block_lookback);
+//   3. publish the tile aggregate and look back (warp 0): over the tiles of
+//      its group of 32, then, if needed, over the descriptors of earlier
+//      groups;
 //   4. publish the inclusive prefix, add the prefix, store.
 // The kernels keep their descriptors in a region of the plan of their own,
 // tagged with the launch's grid id (%gridid: a 64-bit number the driver gives
@@ -31,8 +32,6 @@ namespace {
 constexpr int kMidThreads = 256;
 // Resident CTAs per SM the aligned-buffer kernel is compiled for.
 constexpr int kMidVecCtasPerSm = 8;
-// Descriptors each thread reads per lookback poll: a window of 1024 tiles.
-constexpr int kMidLookbackSlots = 4;
 
 // ------------------------------------------------------------ descriptors
 // One 16-byte word per tile: {lo: the value (u32 or u64), hi: status:2 |
@@ -58,154 +57,142 @@ __device__ __forceinline__ uint64_t grid_id() {
     return g;
 }
 
-// ---------------------------------------------------------- block lookback
-// Shared memory of block_lookback: two rounds of per-warp results.
-template <typename T, int THREADS>
+// ------------------------------------------------------- two-level lookback
+// Tiles form groups of 32. Besides its tile descriptor, the last tile of each
+// group publishes a group descriptor: the group's aggregate as soon as its
+// in-group lookback is done, and the inclusive prefix through the group once
+// its prefix is known. Warp 0 of a tile sums its in-group predecessors back to
+// the nearest inclusive one (one descriptor per lane) and, when none of them
+// is inclusive, adds the prefix of its group: a decoupled lookback over the
+// group descriptors, 32 per poll. Each tile reads at most 31 tile descriptors
+// and the group descriptors back to the nearest inclusive one. A flat
+// lookback, in which every tile reads its predecessors' descriptors directly
+// (one warp, or all warps of the CTA, 128 to 1024 per poll), measured slower
+// from 2^19 elements on: all CTAs of a launch look back at once, and their
+// reads, quadratic in the tile count, queue on the few L2 lines that hold the
+// descriptors.
+constexpr uint32_t kGroupTiles = 32;
+
 struct LookbackSmem {
-    uint32_t incl_pos[THREADS / 32];
-    uint32_t gap_pos[THREADS / 32];
-    T part[THREADS / 32];
-    uint32_t give_up;
+    uint32_t found;    // an inclusive tile was found in the group
+    uint32_t timeout;  // a wait ran past its budget
 };
 
-// Exclusive prefix of tile t > 0 (sum of tiles 0 .. t-1), computed by every
-// thread of the CTA together and returned to all of them. Each poll reads a
-// window of SLOTS * THREADS descriptors below t -- thread i the slots at
-// positions i, i + THREADS, ... (position p is slot t - 1 - p, so a warp's
-// loads are 512 contiguous bytes) -- and needs two barrier rounds: the
-// nearest inclusive prefix, then the nearest slot still not ready below it
-// and the sum of the values up to it. A window of aggregates only moves the
-// walk back by a whole window; a window with a slot not ready is polled again
-// (only the slots not ready are re-read), with back-off after SPIN polls and
-// the plan's wait budget as the bound. Tile 0 publishes an inclusive prefix,
-// so every walk ends there at the latest. The descriptors of a 2^22-element
-// u32 scan (1024 tiles) fit in one window.
-template <typename T, int THREADS, int SLOTS, uint32_t SPIN = 64>
-__device__ T block_lookback(const ScanArgs& a, const ptx::u64x2* desc, uint32_t t, uint64_t gid,
-                            LookbackSmem<T, THREADS>& sm) {
-    constexpr int WARPS = THREADS / 32;
-    constexpr uint32_t WIN = static_cast<uint32_t>(THREADS * SLOTS);
-    constexpr uint32_t kNone = 0xFFFFFFFFu;
-    const uint32_t tid = threadIdx.x;
-    const uint32_t lane = tid & 31u;
-    const uint32_t warp = tid >> 5;
-    T prefix = 0;
-    int64_t top = static_cast<int64_t>(t) - 1;  // slot at position 0
-    uint32_t polls = 0;
+// Warp-level lookback over the 32 descriptors at and below `top` (lane l reads
+// slot top - l when it is at least `floor`). Polls until every slot from top
+// down to the nearest inclusive one (or down to `floor`) is ready; returns
+// whether an inclusive one was found and, in `sum`, the sum of those slots.
+// Gives up after the wait budget, setting timed_out (then `sum` is 0).
+template <typename T, uint32_t SPIN = 64>
+__device__ bool warp_window(const ScanArgs& a, const ptx::u64x2* d, int64_t top, int64_t floor, uint64_t gid,
+                            uint32_t lane, T& sum, bool& timed_out) {
+    const int64_t idx = top - static_cast<int64_t>(lane);
+    bool ready = idx < floor, incl = false;
+    T v = 0;
+    uint32_t polls = 0, backoff = 32;
     uint64_t deadline = 0;
-    uint32_t backoff = 32;
+    timed_out = false;
     while (true) {
-        T val[SLOTS];
-        uint32_t valid = 0, incl = 0, pending = 0;
-#pragma unroll
-        for (int j = 0; j < SLOTS; ++j) {
-            val[j] = 0;
-            if (top - static_cast<int64_t>(tid + j * THREADS) < 0)
-                valid |= 1u << j;  // below slot 0: never summed (slot 0 is inclusive)
-            else
-                pending |= 1u << j;
+        if (!ready) {
+            const ptx::u64x2 w = ptx::ld_relaxed_b128(d + idx);
+            const uint32_t st = MidDesc::status(w, gid);
+            if (st != kNotReady) {
+                ready = true;
+                v = static_cast<T>(w.lo);
+                incl = st == kInclusive;
+            }
         }
-        while (true) {
-#pragma unroll
-            for (int j = 0; j < SLOTS; ++j) {
-                if ((pending >> j) & 1u) {
-                    const ptx::u64x2 w = ptx::ld_relaxed_b128(desc + (top - static_cast<int64_t>(tid + j * THREADS)));
-                    const uint32_t st = MidDesc::status(w, gid);
-                    if (st != kNotReady) {
-                        valid |= 1u << j;
-                        pending &= ~(1u << j);
-                        val[j] = static_cast<T>(w.lo);
-                        if (st == kInclusive) incl |= 1u << j;
-                    }
-                }
-            }
-            // Round 1: the nearest inclusive prefix.
-            uint32_t my = kNone;
-#pragma unroll
-            for (int j = 0; j < SLOTS; ++j)
-                if ((incl >> j) & 1u) my = min(my, tid + j * THREADS);
-            my = __reduce_min_sync(kFullMask, my);
-            if (lane == 0) sm.incl_pos[warp] = my;
-            __syncthreads();
-            uint32_t pinc = kNone;
-#pragma unroll
-            for (int w = 0; w < WARPS; ++w) pinc = min(pinc, sm.incl_pos[w]);
-            // Round 2: the nearest slot not ready below it, and the sum up to it.
-            uint32_t gap = kNone;
-            T part = 0;
-#pragma unroll
-            for (int j = 0; j < SLOTS; ++j) {
-                const uint32_t pos = tid + j * THREADS;
-                if (pos <= pinc) {
-                    if ((valid >> j) & 1u)
-                        part += val[j];
-                    else
-                        gap = min(gap, pos);
-                }
-            }
-            gap = __reduce_min_sync(kFullMask, gap);
-            part = warp_sum(part);
+        const uint32_t inc_mask = __ballot_sync(kFullMask, incl);
+        const uint32_t wait_mask = __ballot_sync(kFullMask, !ready);
+        const uint32_t pinc = inc_mask ? static_cast<uint32_t>(__ffs(inc_mask) - 1) : 32u;
+        const uint32_t need = pinc >= 31u ? kFullMask : (2u << pinc) - 1u;  // lanes 0 .. pinc
+        if ((wait_mask & need) == 0) {
+            sum = warp_sum(lane <= pinc ? v : T(0));
+            return pinc != 32u;
+        }
+        ++polls;
+        if ((polls & 15u) == 1u) {
+            bool expired = false;
             if (lane == 0) {
-                sm.gap_pos[warp] = gap;
-                sm.part[warp] = part;
+                const uint64_t now = ptx::global_timer_ns();
+                if (deadline == 0) deadline = now + a.wait_budget_ns;
+                expired = now > deadline || ld_volatile_u32(&a.hdr->error_flags) != 0;
             }
-            if (tid == 0) {
-                bool give_up = false;
-                if ((polls & 15u) == 1u) {
-                    const uint64_t now = ptx::global_timer_ns();
-                    if (deadline == 0) deadline = now + a.wait_budget_ns;
-                    give_up = now > deadline || ld_volatile_u32(&a.hdr->error_flags) != 0;
-                }
-                sm.give_up = give_up;
+            if (__shfl_sync(kFullMask, expired, 0)) {
+                timed_out = true;
+                sum = 0;
+                return false;
             }
-            __syncthreads();
-            gap = kNone;
-            part = 0;
-#pragma unroll
-            for (int w = 0; w < WARPS; ++w) {
-                gap = min(gap, sm.gap_pos[w]);
-                part += sm.part[w];
-            }
-            if (gap == kNone) {
-                prefix += part;
-                if (pinc != kNone) return prefix;
-                top -= WIN;  // a window of aggregates only
-                polls = 0;
-                break;
-            }
-            if (sm.give_up) {
-                if (tid == 0) raise_error(a.hdr, kErrLookbackTimeout);
-                return prefix;
-            }
-            ++polls;
-            if (polls > SPIN) {
-                __nanosleep(backoff);
-                backoff = backoff < 1024 ? backoff * 2 : 1024;
-            }
+        }
+        if (polls > SPIN) {
+            __nanosleep(backoff);
+            backoff = backoff < 1024 ? backoff * 2 : 1024;
         }
     }
 }
 
 // Publishes tile t's aggregate, resolves its exclusive prefix (carry_in for
 // tile 0) and publishes its inclusive prefix; returns the prefix to every
-// thread. `total` is the tile's sum, known to every thread.
+// thread. `total` is the tile's sum, known to every thread. Warp 0 looks
+// back; a barrier hands its result to the CTA.
 template <typename T>
-__device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint64_t gid, T total,
-                                             LookbackSmem<T, kMidThreads>& sm) {
-    ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
+__device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint64_t gid, T total, LookbackSmem& sm,
+                                             T* s_pre) {
+    ptx::u64x2* d1 = static_cast<ptx::u64x2*>(a.desc);
+    ptx::u64x2* d2 = static_cast<ptx::u64x2*>(a.group_desc);
     const T carry = a.carry_in != nullptr ? *static_cast<const T*>(a.carry_in) : T(0);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t g = t / kGroupTiles;
+    const bool group_last = (t % kGroupTiles) == kGroupTiles - 1;
     if (t == 0) {
-        if (threadIdx.x == 0) {
-            ptx::st_relaxed_b128(desc, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(carry + total)));
+        if (tid == 0) {
+            ptx::st_relaxed_b128(d1, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(carry + total)));
             if (a.carry_out != nullptr && a.num_tiles == 1) *static_cast<T*>(a.carry_out) = carry + total;
         }
         return carry;
     }
-    if (threadIdx.x == 0) ptx::st_relaxed_b128(desc + t, MidDesc::pack(kAggregate, gid, static_cast<uint64_t>(total)));
-    // Tile 0's inclusive prefix holds the carry, so the lookback's sum does too.
-    const T pre = block_lookback<T, kMidThreads, kMidLookbackSlots>(a, desc, t, gid, sm);
-    if (threadIdx.x == 0) {
-        ptx::st_relaxed_b128(desc + t, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
+    if (tid < 32) {
+        const uint32_t lane = tid;
+        if (lane == 0) ptx::st_relaxed_b128(d1 + t, MidDesc::pack(kAggregate, gid, static_cast<uint64_t>(total)));
+        // The tiles of this group before t; tile 0 is inclusive, so group 0
+        // always finds one.
+        T in_sum;
+        bool timed_out;
+        const bool found = warp_window<T>(a, d1, static_cast<int64_t>(t) - 1, static_cast<int64_t>(g) * kGroupTiles,
+                                          gid, lane, in_sum, timed_out);
+        if (lane == 0 && group_last && !timed_out)
+            ptx::st_relaxed_b128(d2 + g, MidDesc::pack(found ? kInclusive : kAggregate, gid,
+                                                       static_cast<uint64_t>(in_sum + total)));
+        // No inclusive tile in the group before t: the prefix of the group, a
+        // decoupled lookback over the group descriptors, 32 per poll.
+        T gsum = 0;
+        if (!found && !timed_out) {
+            int64_t top = static_cast<int64_t>(g) - 1;
+            while (true) {
+                T part;
+                const bool gf = warp_window<T>(a, d2, top, 0, gid, lane, part, timed_out);
+                if (timed_out) break;
+                gsum += part;
+                if (gf || top < 32) break;  // group 0's descriptor is inclusive
+                top -= 32;
+            }
+        }
+        if (lane == 0) {
+            s_pre[0] = in_sum + gsum;
+            sm.timeout = timed_out ? 1u : 0u;
+            sm.found = found ? 1u : 0u;
+        }
+    }
+    __syncthreads();
+    if (sm.timeout != 0) {
+        if (tid == 0) raise_error(a.hdr, kErrLookbackTimeout);
+        return T(0);
+    }
+    const T pre = s_pre[0];
+    if (tid == 0) {
+        ptx::st_relaxed_b128(d1 + t, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
+        if (group_last && sm.found == 0)
+            ptx::st_relaxed_b128(d2 + g, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
         if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
     }
     return pre;
@@ -218,7 +205,8 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
     constexpr int TILE = 16384 / static_cast<int>(sizeof(T));
     constexpr int ITEMS = TILE / kMidThreads;  // 16 u32 or 8 u64: 64 bytes
     __shared__ gps_device::BlockScanStorage<kMidThreads, T> st;
-    __shared__ LookbackSmem<T, kMidThreads> lsm;
+    __shared__ LookbackSmem lsm;
+    __shared__ T s_pre[1];
 
     const uint32_t tid = threadIdx.x;
     const uint32_t t = blockIdx.x;
@@ -235,7 +223,7 @@ __global__ void __launch_bounds__(kMidThreads, 2) mid_scan_kernel(const ScanArgs
     for (int e = 0; e < ITEMS; ++e) sum += v[e];
     T total;
     const T before = gps_device::block_exclusive_scan<kMidThreads>(sum, st, gps_device::Plus(), &total);
-    T run = mid_tile_prefix<T>(a, t, gid, total, lsm) + before;
+    T run = mid_tile_prefix<T>(a, t, gid, total, lsm, s_pre) + before;
 #pragma unroll
     for (int e = 0; e < ITEMS; ++e) {
         const T x = v[e];
@@ -276,7 +264,8 @@ __global__ void __launch_bounds__(kMidThreads, kMidVecCtasPerSm) mid_vec_kernel(
     static_assert(ROWS * WARPS == 32, "one warp scans all (row, warp) totals");
     __shared__ T s_tot[ROWS * WARPS];
     __shared__ T s_off[ROWS][kMidThreads];  // chunk offsets, kept here across the lookback
-    __shared__ LookbackSmem<T, kMidThreads> lsm;
+    __shared__ LookbackSmem lsm;
+    __shared__ T s_pre[1];
 
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31u;
@@ -330,7 +319,7 @@ __global__ void __launch_bounds__(kMidThreads, kMidVecCtasPerSm) mid_vec_kernel(
         for (int r = 0; r < ROWS; ++r) s_off[r][tid] = cs[r] + __shfl_sync(kFullMask, xe, r * WARPS + warp);
     }
 
-    const T base = mid_tile_prefix<T>(a, t, gid, total, lsm);
+    const T base = mid_tile_prefix<T>(a, t, gid, total, lsm, s_pre);
 
     Chunk<T> q[ROWS];
 #pragma unroll
@@ -379,7 +368,9 @@ cudaError_t launch_mid_v(const ScanArgs& a, cudaStream_t stream, LaunchInfo* inf
 
 template <typename T, bool INCL>
 cudaError_t launch_mid_t(const ScanArgs& a, cudaStream_t stream, LaunchInfo* info) {
-    if ((reinterpret_cast<uintptr_t>(a.desc) & 15u) != 0) return cudaErrorInvalidValue;
+    if (((reinterpret_cast<uintptr_t>(a.desc) | reinterpret_cast<uintptr_t>(a.group_desc)) & 15u) != 0 ||
+        a.desc == nullptr || a.group_desc == nullptr)
+        return cudaErrorInvalidValue;
     const bool vec = ((reinterpret_cast<uintptr_t>(a.in) | reinterpret_cast<uintptr_t>(a.out)) & 15u) == 0;
     return vec ? launch_mid_v<T, INCL, true>(a, stream, info) : launch_mid_v<T, INCL, false>(a, stream, info);
 }

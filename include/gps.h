@@ -222,20 +222,23 @@ gps_status gps_plan_set_stall(gps_plan plan, uint32_t mode, uint32_t period, uin
  * which the CUDA part only shows in its EmulatedDeadlocking test. */
 gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
 
-/* Integer scans of at most max_n elements (default and maximum: 64 KB of
- * input, 16384 u32 or 8192 u64) run in a single CTA instead of the
- * persistent multi-CTA kernels, whose pipeline costs a fixed few
- * microseconds; 0 sends every scan to the chained scan / reduce-then-scan
- * kernels. Forced-stall and fallback modes always use the multi-CTA kernels. */
+/* Integer scans of at most max_n elements (maximum: 64 KB of input, 16384
+ * u32 or 8192 u64) run in a single CTA instead of the multi-CTA kernels.
+ * Default: 64 KB on GPS_ALGO_RTS plans; 0 on GPS_ALGO_CSDL plans, whose
+ * one-tile-per-CTA kernel (below) is as fast or faster at these sizes.
+ * 0 sends every scan to the multi-CTA kernels. Forced-stall and fallback
+ * modes always use the multi-CTA kernels. */
 gps_status gps_plan_set_small_max(gps_plan plan, uint64_t max_n);
 
 /* Integer scans on a GPS_ALGO_CSDL plan above the one-CTA size and of at
- * most max_n elements (default: 4 MB of input, 2^20 u32 or 2^19 u64) run
- * as one 16 KB tile per CTA -- a single-pass chained scan without the
- * persistent kernel's pipeline, whose latency dominates at these sizes;
+ * most max_n elements (default: 48 MB of input, 12 x 2^20 u32 or 6 x 2^20
+ * u64) run as one 16 KB tile per CTA -- a single-pass chained scan without
+ * the persistent kernel's pipeline, whose latency dominates at these sizes;
  * larger ones run on the persistent L2-buffered kernel. 0 sends them all to
  * the persistent kernel. Forced-stall and fallback modes always use the
- * persistent kernel. */
+ * persistent kernel. The kernel takes its tile ids from the block index and
+ * relies on the hardware starting lower-numbered blocks first, as CUB's
+ * decoupled lookback does; its waits are bounded all the same. */
 gps_status gps_plan_set_mid_max(gps_plan plan, uint64_t max_n);
 
 /* Lookback statistics gathered while forced-stall mode is on. Synchronizes

@@ -33,7 +33,7 @@ from gpuprefixsums_gb300 import Plan
 pytestmark = pytest.mark.gpu
 
 PART = 4096          # the reference's tile (ChainedScanDecoupledLookbackDispatcher.cuh:13-18)
-ONE_CTA_MAX = 16384  # u32 elements the one-CTA kernel takes by default
+ONE_CTA_MAX = 16384  # most u32 elements the one-CTA kernel takes (64 KB)
 
 
 def _ref():
@@ -49,8 +49,7 @@ def _paths(n):
 
 def _plan(path, max_n, algo="csdl"):
     plan = Plan(algo, "u32", max_n=max_n)
-    if path != "one_cta":
-        plan.set_small_max(0)
+    plan.set_small_max(ONE_CTA_MAX if path == "one_cta" else 0)
     if path == "mid":
         plan.set_mid_max(max_n)   # one tile per CTA at every size
     if path == "persistent":
