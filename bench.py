@@ -67,11 +67,13 @@ def parse_args():
     p.add_argument("--no-compare", action="store_true",
                    help="only the timed scans (for profiling): no copy/CUB/RTS/e2e/CPU legs")
     p.add_argument("--no-extras", action="store_true", help="skip the batched, fp32 and mixed workloads")
-    p.add_argument("--profile-case", choices=["batched", "f32c", "select", "struct", "mid"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "f32c", "select", "struct", "mid", "f32c_batched",
+                                              "u64_batched"], default=None,
                    help="launch one small case three times and exit (ncu captures): 1024 of the batched "
                         "workload's segments, 2^26 compensated-f32 elements, a select of 2^26 u32 by "
-                        "Bernoulli(0.3) flags, an inclusive scan of 2^24 structs of four u32, or an "
-                        "exclusive u32 scan of 2^20 elements (the one-tile-per-CTA kernel)")
+                        "Bernoulli(0.3) flags, an inclusive scan of 2^24 structs of four u32, an "
+                        "exclusive u32 scan of 2^20 elements (the one-tile-per-CTA kernel), or the first "
+                        "1000 compensated-f32 / u64 segments of the mixed workload")
     p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--clock-soak-s", type=float, default=1.0,
                    help="seconds of untimed steps sampled for clocks right before the timed region")
@@ -830,6 +832,21 @@ def run_profile_case(args):
                 out, cnt = plan.select(x, fl)
             plan.check()
         out = out[:int(cnt.item())]
+    elif args.profile_case in ("f32c_batched", "u64_batched"):
+        name = args.profile_case.split("_")[0]
+        lengths = zipf_lengths(10_000, 1.2, 32, 2 ** 22, seed=5)
+        kinds = np.random.default_rng(55).integers(0, 3, size=10_000)
+        ls = lengths[kinds == (2 if name == "f32c" else 1)][:1000]
+        offs = np.concatenate([[0], np.cumsum(ls)]).astype(np.uint32)
+        n = int(offs[-1])
+        x = torch.randn(n, device="cuda") if name == "f32c" else \
+            torch.randint(-2 ** 63, 2 ** 63 - 1, (n,), dtype=torch.int64, device="cuda")
+        d_off = torch.from_numpy(offs.view(np.int32)).cuda()
+        with Plan("csdl", name, max_n=n) as plan:
+            for _ in range(3):
+                out = plan.scan_segmented(x, d_off)
+            plan.check()
+        out = out.float()
     elif args.profile_case == "mid":
         n = 1 << 20
         x = torch.randint(0, 256, (n,), dtype=torch.int32, device="cuda")

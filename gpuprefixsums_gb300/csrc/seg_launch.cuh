@@ -12,8 +12,11 @@ namespace gps {
 // block (whose per-thread prefixes and head bitmaps grow with the state size
 // and the unit), taken as 4 reduce-pass + 9 scan-pass stages when 13 fit
 // (measured on GB300: 4 + 9 beats 5 + 8 by 3-8% on the batched workloads),
-// else 4 + 8, 3 + 8, 3 + 7, 3 + 6. The unit (1 or 4 tiles) and the CTA count come from
-// the plan's launch configuration (GenericConfig).
+// else 4 + 8, 4 + 7, 3 + 7, 3 + 6. Four reduce-pass stages matter more than
+// a scan-pass stage: with 11 stages, 4 + 7 instead of 3 + 8 took the batched
+// u64 scan (3312 segments, 357 M elements) from 4.98 to 6.22 TB/s, and 3 + 8
+// took batched FP32 from 6.17 down to 4.79. The unit (1 or 4 tiles) and the
+// CTA count come from the plan's launch configuration (GenericConfig).
 constexpr int kSegWarps = 4;
 constexpr int kSegQueue = 6;
 constexpr size_t kMaxSmem = 232448;
@@ -25,8 +28,8 @@ struct SegStages {
     static constexpr bool k12 = seg_smem_bytes<Op, RW, 4, 8, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr bool k11 = seg_smem_bytes<Op, RW, 3, 8, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr bool k10 = seg_smem_bytes<Op, RW, 3, 7, kSegQueue, G, SEG>() <= kMaxSmem;
-    static constexpr int RS = (k13 || k12) ? 4 : 3;
-    static constexpr int SS = k13 ? 9 : (k12 || k11) ? 8 : k10 ? 7 : 6;
+    static constexpr int RS = (k13 || k12 || k11) ? 4 : 3;
+    static constexpr int SS = k13 ? 9 : k12 ? 8 : (k11 || k10) ? 7 : 6;
     static_assert(seg_smem_bytes<Op, RW, RS, SS, kSegQueue, G, SEG>() <= kMaxSmem, "227 KB per CTA");
 };
 
