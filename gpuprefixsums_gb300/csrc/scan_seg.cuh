@@ -850,8 +850,18 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
                 break;
             }
             T* sb = sbuf + static_cast<size_t>(s) * TILE;
+            // Scans whose state is wider than an element (the compensated
+            // one) keep a single, rolled copy of the per-item chain, the
+            // head-aware one: the kernel is sensitive to its code size (every
+            // SM sub-partition runs a reduce and a finalize warp next to the
+            // other roles). Measured on GB300, 3367 segments of 340 M
+            // elements: two unrolled copies (head-free and head-aware) 2.81
+            // TB/s, one unrolled head-aware copy 3.43, one copy rolled over
+            // chunk pairs 4.69; unsegmented, the rolled chain 6.17 against
+            // 5.82 unrolled.
+            constexpr bool kRolled = sizeof(S) > sizeof(T);
             T v[ITEMS];
-            load_row(sb, t, f, v);
+            if constexpr (!kRolled) load_row(sb, t, f, v);
             if (k == 0) {
                 // The unit's prefix (which also orders this warp after the
                 // head warp's bits), and the per-thread states (ustates).
@@ -869,19 +879,50 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             const S pre = ctrl->tpre[q][entry_at(j)];
             const bool pf = SEG && ctrl->tflag[SEG ? q : 0][SEG ? j : 0] != 0;
             const S base = pf ? pre : Op::combine(run, pre);
-            // Segmented scans whose state is wider than an element (the
-            // compensated one) keep a single copy of the per-item chain, the
-            // head-aware one, at a few selects per item: with two unrolled
-            // copies of its TwoSums every role of the kernel ran 1.6-2.8x
-            // slower than in the unsegmented kernel (per-tile timestamps on
-            // GB300); one copy took 3367 segments of 340 M elements from 2.90
-            // to 3.47 TB/s.
-            constexpr bool kOneCopy = SEG && sizeof(S) > sizeof(T);
-            if (SEG && (kOneCopy || __any_sync(kFullMask, hb != 0u)))
-                thread_outputs<Op, ITEMS, true, INCL>(v, base, hb);
-            else
-                thread_outputs<Op, ITEMS, false, INCL>(v, base, 0u);
-            store_row(sb, t, f, v);
+            if constexpr (kRolled) {
+                // One head-aware chain, run as a rolled loop over pairs of
+                // 16-byte chunks, in place in the stage (or in global memory
+                // for the last, partial row).
+                const uint32_t rit = f / SPLIT, sub = f % SPLIT;
+                const uint64_t row = static_cast<uint64_t>(t) * ROWS + rit;
+                S st = base;
+                if (row < rows_full) {
+                    T* rp = sb + rit * ROW;
+#pragma unroll 1
+                    for (int cp = 0; cp < CHUNKS; cp += 2) {
+                        const int p0 = (static_cast<int>(sub) * CHUNKS + cp) ^ static_cast<int>(rit & 7u);
+                        const int p1 = (static_cast<int>(sub) * CHUNKS + cp + 1) ^ static_cast<int>(rit & 7u);
+                        Chunk<T> q0 = *reinterpret_cast<const Chunk<T>*>(rp + p0 * EPC);
+                        Chunk<T> q1 = *reinterpret_cast<const Chunk<T>*>(rp + p1 * EPC);
+                        const uint32_t hbits = hb >> (cp * EPC);
+#pragma unroll
+                        for (int e = 0; e < 2 * EPC; ++e) {
+                            T& x = e < EPC ? q0.v[e] : q1.v[e - EPC];
+                            const S before = ((hbits >> e) & 1u) ? Op::zero() : st;
+                            st = Op::acc(before, x);
+                            x = INCL ? Op::out(st) : Op::out(before);
+                        }
+                        *reinterpret_cast<Chunk<T>*>(rp + p0 * EPC) = q0;
+                        *reinterpret_cast<Chunk<T>*>(rp + p1 * EPC) = q1;
+                    }
+                } else if (row == rows_full) {
+                    const T* gi = static_cast<const T*>(a.in) + row * ROW + sub * ITEMS;
+                    T* go = static_cast<T*>(a.out) + row * ROW + sub * ITEMS;
+#pragma unroll 1
+                    for (uint32_t e = 0; sub * ITEMS + e < tail && e < static_cast<uint32_t>(ITEMS); ++e) {
+                        const T x = gi[e];
+                        const S before = ((hb >> e) & 1u) ? Op::zero() : st;
+                        st = Op::acc(before, x);
+                        go[e] = INCL ? Op::out(st) : Op::out(before);
+                    }
+                }
+            } else {
+                if (SEG && __any_sync(kFullMask, hb != 0u))
+                    thread_outputs<Op, ITEMS, true, INCL>(v, base, hb);
+                else
+                    thread_outputs<Op, ITEMS, false, INCL>(v, base, 0u);
+                store_row(sb, t, f, v);
+            }
             ptx::fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
