@@ -58,7 +58,6 @@ struct SelCtrl {
     uint64_t upre[kSelQ];
     uint32_t r_wtot[2][kSelWarps];
     uint32_t tpre[kSelQ][kSelG][kSelRole];  // count before each thread within its unit
-    uint32_t ttot[kSelQ][kSelG];             // count of each tile
 };
 
 template <typename V>
@@ -370,7 +369,6 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
                 tot += x;
             }
             ctrl->tpre[q][k][r] = unit_cnt + wpre + (winc - cnt);
-            if (r == 0) ctrl->ttot[q][k] = tot;
             unit_cnt += tot;
             if (k == G - 1) {
                 if (r == 0) {
@@ -384,9 +382,20 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
         }
     }
     // ======================================================== finalize
+    // Thread f owns row f of each tile (ITEMS consecutive elements), so warp
+    // w owns the 32 * ITEMS consecutive elements of rows 32w .. 32w + 31 and
+    // compacts them into its own slice of the staging tile: each thread puts
+    // its selected values at its count-prefix within the warp (from the reduce
+    // pass), then the warp copies its run out with consecutive lanes on
+    // consecutive output elements. Only the warp synchronises, no barrier
+    // between the finalize warps. (A staging tile shared by the four warps
+    // needed three barriers per tile; ranking the warp's elements 32 at a
+    // time by ballots ran a dependent chain per step and was 2x slower.)
     else {
         const uint32_t f = tid - kWarpFinal * 32;
+        const uint32_t fw = warp - kWarpFinal;
         const uint32_t rot = f & 7u;
+        V* wst = ostage + fw * 32u * ITEMS;  // this warp's staging slice
         uint64_t run = 0;  // the unit's output position
         for (uint32_t sn = 0;; ++sn) {
             const int s = static_cast<int>(sn % SS);
@@ -395,10 +404,7 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
             const int q = static_cast<int>(i % Q);
             const bool ok = wait1(&ctrl->sfull[s], (sn / SS) & 1u, long_budget);
             const uint32_t t = ok ? ctrl->s_tile[s] : kTileEnd;
-            // All finalize threads stop together (the end, or a wait that ran
-            // out anywhere): the staging barriers below then never strand a
-            // warp.
-            if (named_bar_or(3, kSelRole, t == kTileEnd)) {
+            if (__any_sync(kFullMask, t == kTileEnd)) {
                 if (!ok) raise_error(a.hdr, kErrPipelineTimeout);
                 break;
             }
@@ -444,23 +450,23 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
             uint32_t cpre[CHUNKS];
             uint32_t total;
             rotated_chunk_prefix<uint32_t, CHUNKS>(cs, rrot, cpre, total);
-            const uint32_t tile_base = ctrl->tpre[q][k][0];
-            const uint32_t mine = ctrl->tpre[q][k][f] - tile_base;
-            const uint32_t tile_cnt = ctrl->ttot[q][k];
-            // The staging tile may still be read by the previous copy-out.
-            ptx::named_bar_sync(2, kSelRole);
+            const uint32_t warp_base = ctrl->tpre[q][k][fw * 32u];
+            const uint32_t mine = ctrl->tpre[q][k][f] - warp_base;
+            const uint32_t warp_cnt = __shfl_sync(kFullMask, mine + total, 31);
+            // The slice may still be read by this warp's previous copy-out.
+            __syncwarp();
 #pragma unroll
             for (int c8 = 0; c8 < CHUNKS; ++c8) {
                 const uint32_t l = (c8 + rrot) & (CHUNKS - 1);
                 uint32_t pos = mine + cpre[c8];
 #pragma unroll
                 for (int e = 0; e < EPC; ++e) {
-                    if ((mask >> (l * EPC + e)) & 1u) ostage[pos++] = v[c8 * EPC + e];
+                    if ((mask >> (l * EPC + e)) & 1u) wst[pos++] = v[c8 * EPC + e];
                 }
             }
-            ptx::named_bar_sync(2, kSelRole);
-            V* out = static_cast<V*>(a.out) + run + tile_base;
-            for (uint32_t x = f; x < tile_cnt; x += kSelRole) out[x] = ostage[x];
+            __syncwarp();
+            V* out = static_cast<V*>(a.out) + run + warp_base;
+            for (uint32_t x = lane; x < warp_cnt; x += 32u) out[x] = wst[x];
             if (k == G - 1 && lane == 0) ptx::mbar_arrive(&ctrl->ufree[q]);
         }
     }
