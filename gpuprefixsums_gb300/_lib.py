@@ -51,10 +51,11 @@ SIGNATURES = [
     ("gps_scan_host", _INT, [_P, _INT, _P, _P, _U64, _P]),
     ("gps_scan_segmented", _INT, [_P, _INT, _P, _P, _U64, _P, _U64, _P]),
     ("gps_select_flagged", _INT, [_P, _P, _P, _P, _U64, _P, _P]),
-    ("gps_plan_autotune", _INT, [_P, _INT, _P, _P, _U64, _P, _U64, _P, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
-    ("gps_plan_set_generic_config", _INT, [_P, _INT, _U64, _U32, _U32]),
+    ("gps_plan_autotune", _INT, [_P, _INT, _P, _P, _U64, _P, _U64, _P, ctypes.POINTER(_U32), ctypes.POINTER(_U32),
+                                 ctypes.POINTER(_U32)]),
+    ("gps_plan_set_generic_config", _INT, [_P, _INT, _U64, _U32, _U32, _U32]),
     ("gps_plan_generic_config", _INT, [_P, _INT, _U64, ctypes.POINTER(_U32), ctypes.POINTER(_U32),
-                                       ctypes.POINTER(_INT)]),
+                                       ctypes.POINTER(_U32), ctypes.POINTER(_INT)]),
     ("gps_plan_check", _INT, [_P, _P]),
     ("gps_plan_set_wait_budget", _INT, [_P, _U64]),
     ("gps_plan_set_stall", _INT, [_P, _U32, _U32, _U32, _U32, _U32]),

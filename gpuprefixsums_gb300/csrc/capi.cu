@@ -121,6 +121,19 @@ cudaError_t launch_generic(gps_dtype dtype, bool inclusive, const gps::ScanArgs&
     }
     return cudaErrorInvalidValue;
 }
+// Whether a launch configuration's kernels exist for the element type (two
+// threads per row do not fit every type's shared memory).
+bool generic_config_fits(gps_dtype dtype, const gps::GenericConfig& cfg) {
+    if (cfg.split == 1) return true;
+    switch (dtype) {
+        case GPS_DTYPE_U32: return gps::seg_u32_x2_fits(cfg.unit);
+        case GPS_DTYPE_U64: return gps::seg_u64_x2_fits(cfg.unit);
+        case GPS_DTYPE_F32: return gps::seg_f32_x2_fits(cfg.unit);
+        case GPS_DTYPE_F32_COMPENSATED: return gps::seg_f32c_x2_fits(cfg.unit);
+        case GPS_DTYPE_U32X4: return gps::seg_u32x4_x2_fits(cfg.unit);
+    }
+    return false;
+}
 bool valid_algo(int a) { return a == GPS_ALGO_CSDL || a == GPS_ALGO_RTS; }
 bool valid_kind(int k) { return k == GPS_SCAN_EXCLUSIVE || k == GPS_SCAN_INCLUSIVE; }
 
@@ -170,13 +183,40 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     return GPS_OK;
 }
 
+// Order-free 64-bit hash of a buffer (the sum of x_i * (2i + 1) over its
+// 8-byte words, mod 2^64), added into *h: the autotuner compares each launch
+// configuration's output with the first one's without keeping a copy.
+__global__ void hash_words_kernel(const uint64_t* w, uint64_t nwords, const uint8_t* tail, uint32_t tail_bytes,
+                                  unsigned long long* h) {
+    uint64_t acc = 0;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < nwords;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        acc += w[i] * (2 * i + 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (uint32_t b = 0; b < tail_bytes; ++b) acc += static_cast<uint64_t>(tail[b]) * (2 * (nwords + b) + 1);
+#pragma unroll
+    for (int m = 16; m; m >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, m);
+    if ((threadIdx.x & 31u) == 0) atomicAdd(h, static_cast<unsigned long long>(acc));
+}
+
+// Hash of `bytes` bytes at d (8-byte aligned) into *d_hash, on `stream`.
+cudaError_t hash_buffer(const void* d, uint64_t bytes, unsigned long long* d_hash, cudaStream_t stream) {
+    cudaError_t err = cudaMemsetAsync(d_hash, 0, sizeof(*d_hash), stream);
+    if (err != cudaSuccess) return err;
+    const uint64_t nwords = bytes / 8;
+    hash_words_kernel<<<304, 256, 0, stream>>>(static_cast<const uint64_t*>(d), nwords,
+                                                static_cast<const uint8_t*>(d) + nwords * 8,
+                                                static_cast<uint32_t>(bytes % 8), d_hash);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 namespace gps {
 size_t dtype_size(gps_dtype dtype) { return dtype == GPS_DTYPE_U64 ? 8 : dtype == GPS_DTYPE_U32X4 ? 16 : 4; }
 GenericConfig default_generic_config(uint64_t n, uint32_t tile_elems, int num_sms) {
     const uint64_t units4 = (n + 4ull * tile_elems - 1) / (4ull * tile_elems);
-    return units4 >= 2ull * static_cast<uint64_t>(num_sms) ? GenericConfig{4, 1} : GenericConfig{1, 1};
+    return units4 >= 2ull * static_cast<uint64_t>(num_sms) ? GenericConfig{4, 1, 1} : GenericConfig{1, 1, 1};
 }
 void record_error(const char* msg) { g_last_error = msg; }
 }  // namespace gps
@@ -403,7 +443,7 @@ gps_status gps_scan_segmented(gps_plan p, gps_scan_kind kind, const void* d_in, 
 
 gps_status gps_plan_autotune(gps_plan p, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
                              const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream,
-                             uint32_t* out_unit, uint32_t* out_ctas) {
+                             uint32_t* out_unit, uint32_t* out_ctas, uint32_t* out_threads_per_row) {
     gps::ScanArgs a;
     gps::SegArgs sg;
     gps_status st = prepare_generic(p, kind, d_in, d_out, n, d_offsets, num_segments, &a, &sg);
@@ -414,18 +454,38 @@ gps_status gps_plan_autotune(gps_plan p, gps_scan_kind kind, const void* d_in, v
     cudaError_t err = cudaStreamIsCapturing(s, &cap);
     if (err != cudaSuccess) return cuda_fail(err, "cudaStreamIsCapturing");
     if (cap != cudaStreamCaptureStatusNone) return fail(GPS_ERR_INVALID_ARGUMENT, "autotuning cannot be captured");
+    if (d_in == d_out) return fail(GPS_ERR_INVALID_ARGUMENT, "autotuning needs separate input and output buffers");
     const bool seg = d_offsets != nullptr;
+    // Integer results do not depend on the launch configuration: every
+    // candidate's output must hash like the first one's, or the candidate is
+    // not taken. (Floating-point results differ in rounding from one
+    // configuration to the next.)
+    const bool check = !is_float(p->dtype);
+    unsigned long long* d_hash = reinterpret_cast<unsigned long long*>(p->carries);
+    const uint64_t out_bytes = n * gps::dtype_size(p->dtype);
+    unsigned long long first_hash = 0, hash = 0;
+    bool have_first = false;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);
-    int best = -1;
+    int best = -1, rejected = 0;
     float best_ms = 0.0f;
     for (int c = 0; c < gps::kNumGenericCandidates && err == cudaSuccess; ++c) {
         const gps::GenericConfig& cfg = gps::kGenericCandidates[c];
+        if (!generic_config_fits(p->dtype, cfg)) continue;  // this kernel shape does not fit the type
         gps::LaunchInfo info{};
         const gps::SegArgs* sgp = seg ? &sg : nullptr;
         const bool incl = kind == GPS_SCAN_INCLUSIVE;
         err = launch_generic(p->dtype, incl, a, sgp, cfg, p->num_sms, s, &info);  // warm-up
+        if (err == cudaSuccess && check) {
+            err = hash_buffer(d_out, out_bytes, d_hash, s);
+            if (err == cudaSuccess) err = cudaMemcpyAsync(&hash, d_hash, sizeof(hash), cudaMemcpyDeviceToHost, s);
+            if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+            if (err == cudaSuccess && !have_first) {
+                first_hash = hash;
+                have_first = true;
+            }
+        }
         if (err == cudaSuccess) err = cudaEventRecord(e0, s);
         for (int r = 0; r < 3 && err == cudaSuccess; ++r)
             err = launch_generic(p->dtype, incl, a, sgp, cfg, p->num_sms, s, &info);
@@ -433,7 +493,12 @@ gps_status gps_plan_autotune(gps_plan p, gps_scan_kind kind, const void* d_in, v
         if (err == cudaSuccess) err = cudaEventSynchronize(e1);
         float ms = 0.0f;
         if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-        if (err == cudaSuccess && (best < 0 || ms < best_ms)) {
+        if (err != cudaSuccess) break;
+        if (check && hash != first_hash) {
+            ++rejected;
+            continue;
+        }
+        if (best < 0 || ms < best_ms) {
             best = c;
             best_ms = ms;
         }
@@ -441,30 +506,48 @@ gps_status gps_plan_autotune(gps_plan p, gps_scan_kind kind, const void* d_in, v
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (err != cudaSuccess) return cuda_fail(err, "autotuning");
+    if (best < 0) return fail(GPS_ERR_CUDA, "autotuning: no launch configuration ran");
+    // Leave a correct result in d_out, from the chosen configuration.
+    err = launch_generic(p->dtype, kind == GPS_SCAN_INCLUSIVE, a, seg ? &sg : nullptr, gps::kGenericCandidates[best],
+                         p->num_sms, s, &p->last_launch);
+    if (err != cudaSuccess) return cuda_fail(err, "autotuning");
     p->tuned[seg ? 1 : 0][size_class(n)] = static_cast<int8_t>(best);
     if (out_unit) *out_unit = gps::kGenericCandidates[best].unit;
     if (out_ctas) *out_ctas = gps::kGenericCandidates[best].ctas_div;
-    return gps_plan_check(p, stream);
+    if (out_threads_per_row) *out_threads_per_row = gps::kGenericCandidates[best].split;
+    st = gps_plan_check(p, stream);
+    if (st != GPS_OK) return st;
+    if (rejected != 0)
+        return fail(GPS_ERR_CUDA, "autotuning: %d launch configuration(s) gave a different result and were not taken",
+                    rejected);
+    return GPS_OK;
 }
 
-gps_status gps_plan_set_generic_config(gps_plan p, int segmented, uint64_t n, uint32_t unit, uint32_t ctas_div) {
+gps_status gps_plan_set_generic_config(gps_plan p, int segmented, uint64_t n, uint32_t unit, uint32_t ctas_div,
+                                       uint32_t threads_per_row) {
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     for (int c = 0; c < gps::kNumGenericCandidates; ++c) {
-        if (gps::kGenericCandidates[c].unit == unit && gps::kGenericCandidates[c].ctas_div == ctas_div) {
+        const gps::GenericConfig& g = gps::kGenericCandidates[c];
+        if (g.unit == unit && g.ctas_div == ctas_div && g.split == threads_per_row) {
+            if (!generic_config_fits(p->dtype, g))
+                return fail(GPS_ERR_UNSUPPORTED, "%u threads per row with units of %u tiles do not fit one CTA for this "
+                            "element type", threads_per_row, unit);
             p->tuned[segmented ? 1 : 0][size_class(n)] = static_cast<int8_t>(c);
             return GPS_OK;
         }
     }
-    return fail(GPS_ERR_INVALID_ARGUMENT, "no launch configuration with %u tiles per unit and CTA divisor %u", unit,
-                ctas_div);
+    return fail(GPS_ERR_INVALID_ARGUMENT,
+                "no launch configuration with %u tiles per unit, CTA divisor %u and %u threads per row", unit, ctas_div,
+                threads_per_row);
 }
 
 gps_status gps_plan_generic_config(gps_plan p, int segmented, uint64_t n, uint32_t* out_unit, uint32_t* out_ctas_div,
-                                   int* out_tuned) {
+                                   uint32_t* out_threads_per_row, int* out_tuned) {
     if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
     const gps::GenericConfig cfg = generic_config(p, segmented != 0, n);
     if (out_unit) *out_unit = cfg.unit;
     if (out_ctas_div) *out_ctas_div = cfg.ctas_div;
+    if (out_threads_per_row) *out_threads_per_row = cfg.split;
     if (out_tuned) *out_tuned = p->tuned[segmented ? 1 : 0][size_class(n)] >= 0 ? 1 : 0;
     return GPS_OK;
 }

@@ -130,14 +130,18 @@ struct RowMaps {
 cudaError_t encode_row_maps(const void* in, void* out, uint64_t n, uint32_t elem_size, RowMaps* maps);
 
 // Launch configuration of the generic kernel: tiles per lookback unit (1 or
-// 4; the unit is what one CTA takes from the work counter) and the CTA count
-// as a fraction of the resident maximum (1 = all, 2 = half).
+// 4; the unit is what one CTA takes from the work counter), the CTA count as
+// a fraction of the resident maximum (1 = all, 2 = half), and threads per
+// 128-byte row of a tile (1: 4 reduce and 4 finalize warps, each thread
+// scanning 128 bytes; 2: 8 and 8, each thread scanning 64 bytes).
 struct GenericConfig {
     uint32_t unit;
     uint32_t ctas_div;
+    uint32_t split;
 };
-constexpr GenericConfig kGenericCandidates[] = {{4, 1}, {1, 1}, {4, 2}, {1, 2}};
-constexpr int kNumGenericCandidates = 4;
+constexpr GenericConfig kGenericCandidates[] = {{4, 1, 1}, {1, 1, 1}, {4, 2, 1}, {1, 2, 1},
+                                                {4, 1, 2}, {1, 1, 2}, {4, 2, 2}, {1, 2, 2}};
+constexpr int kNumGenericCandidates = 8;
 // Untuned choice: units of 4 tiles once there are at least two such units
 // per SM, else single-tile units (more CTAs busy on small inputs).
 GenericConfig default_generic_config(uint64_t n, uint32_t tile_elems, int num_sms);
@@ -154,6 +158,25 @@ cudaError_t launch_seg_f32c(bool inclusive, const ScanArgs& a, const SegArgs* sg
                             int num_sms, cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_seg_u32x4(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
                              int num_sms, cudaStream_t stream, LaunchInfo* info);
+// The same with two threads per row (cfg.split == 2), in translation units of
+// their own (seg_*_x2.cu); cudaErrorNotSupported when that kernel shape does
+// not fit one CTA's shared memory for the type.
+cudaError_t launch_seg_u32_x2(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                              int num_sms, cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_u64_x2(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                              int num_sms, cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_f32_x2(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                              int num_sms, cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_f32c_x2(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                               int num_sms, cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_seg_u32x4_x2(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
+                                int num_sms, cudaStream_t stream, LaunchInfo* info);
+// Whether the two-threads-per-row kernels of a unit size fit one CTA.
+bool seg_u32_x2_fits(uint32_t unit);
+bool seg_u64_x2_fits(uint32_t unit);
+bool seg_f32_x2_fits(uint32_t unit);
+bool seg_f32c_x2_fits(uint32_t unit);
+bool seg_u32x4_x2_fits(uint32_t unit);
 
 // Stream compaction by flag bytes (select.cu): elements per tile for an
 // element size, and the launch. a.carry_out receives the count (uint64).

@@ -33,13 +33,11 @@ template <>
 __device__ __forceinline__ float shfl_up_any(float s, uint32_t d) { return __shfl_up_sync(0xFFFFFFFFu, s, d); }
 
 // ------------------------------------------------------------- integers
-// kSplit: threads per 128-byte row of a tile (1: 4 + 4 compute warps).
 template <typename U>
 struct OpInt {
     using T = U;
     using S = U;
     using C = U;
-    static constexpr int kSplit = 1;
     static constexpr bool kPackedRowSum = false;
     __device__ static S zero() { return 0; }
     __device__ static S lift(T x) { return x; }
@@ -71,7 +69,6 @@ struct OpF32 {
     using T = float;
     using S = float;
     using C = float;
-    static constexpr int kSplit = 1;
     static constexpr bool kPackedRowSum = false;
     __device__ static S zero() { return 0.0f; }
     __device__ static S lift(T x) { return x; }
@@ -136,10 +133,6 @@ struct OpF32C {
     using T = float;
     using S = F2;
     using C = double;
-    // One thread per 128-byte row. (Two per row -- 8 reduce and 8 finalize
-    // warps of 16 items -- measured 25% slower on GB300: the per-thread
-    // prefixes double and leave room for fewer stages.)
-    static constexpr int kSplit = 1;
     // The reduce pass sums a row as two half-chains (even and odd items) in
     // packed FP32x2 TwoSums: half the instructions of one chain.
     static constexpr bool kPackedRowSum = true;
@@ -225,7 +218,6 @@ struct OpU32x4 {
     using T = uint4;
     using S = uint4;
     using C = uint4;
-    static constexpr int kSplit = 1;
     static constexpr bool kPackedRowSum = false;
     static constexpr int kDescWords = 2;
     __device__ static S zero() { return make_uint4(0u, 0u, 0u, 0u); }

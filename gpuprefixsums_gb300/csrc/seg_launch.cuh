@@ -21,22 +21,28 @@ constexpr int kSegWarps = 4;
 constexpr int kSegQueue = 6;
 constexpr size_t kMaxSmem = 232448;
 
-template <class Op, int G, bool SEG>
+template <class Op, int G, bool SEG, int SPLIT>
 struct SegStages {
-    static constexpr int RW = kSegWarps * Op::kSplit;  // warps per role
+    static constexpr int RW = kSegWarps * SPLIT;  // warps per role
     static constexpr bool k13 = seg_smem_bytes<Op, RW, 4, 9, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr bool k12 = seg_smem_bytes<Op, RW, 4, 8, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr bool k11 = seg_smem_bytes<Op, RW, 3, 8, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr bool k10 = seg_smem_bytes<Op, RW, 3, 7, kSegQueue, G, SEG>() <= kMaxSmem;
     static constexpr int RS = (k13 || k12 || k11) ? 4 : 3;
     static constexpr int SS = k13 ? 9 : k12 ? 8 : (k11 || k10) ? 7 : 6;
-    static_assert(seg_smem_bytes<Op, RW, RS, SS, kSegQueue, G, SEG>() <= kMaxSmem, "227 KB per CTA");
+    // Two threads per row double the per-thread prefixes: some types do not
+    // fit 9 stages then, and that shape is not offered for them.
+    static constexpr bool kFits = seg_smem_bytes<Op, RW, RS, SS, kSegQueue, G, SEG>() <= kMaxSmem;
+    static_assert(kFits || SPLIT > 1, "227 KB per CTA");
 };
 
-template <class Op, bool INCL, bool SEG, int UNIT>
+template <class Op, bool INCL, bool SEG, int UNIT, int SPLIT>
 cudaError_t launch_seg_t(const ScanArgs& a, const SegArgs& sg, const GenericConfig& cfg, int num_sms,
                          cudaStream_t stream, LaunchInfo* info) {
-    using St = SegStages<Op, UNIT, SEG>;
+    using St = SegStages<Op, UNIT, SEG, SPLIT>;
+    if constexpr (!St::kFits) {
+        return cudaErrorNotSupported;
+    } else {
     auto kern = scan_seg_kernel<Op, St::RW, St::RS, St::SS, kSegQueue, UNIT, INCL, SEG>;
     constexpr size_t smem = seg_smem_bytes<Op, St::RW, St::RS, St::SS, kSegQueue, UNIT, SEG>();
     constexpr int threads = SegShape<Op, St::RW>::kThreads;
@@ -52,25 +58,28 @@ cudaError_t launch_seg_t(const ScanArgs& a, const SegArgs& sg, const GenericConf
     if (info) *info = LaunchInfo{grid, threads, smem};
     kern<<<grid, threads, smem, stream>>>(a, sg, maps.in, maps.out);
     return cudaGetLastError();
+    }
 }
 
-template <class Op, int UNIT>
+template <class Op, int UNIT, int SPLIT>
 cudaError_t launch_seg_unit(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
                             int num_sms, cudaStream_t stream, LaunchInfo* info) {
     const SegArgs none{nullptr, 0};
     if (sg != nullptr)
-        return inclusive ? launch_seg_t<Op, true, true, UNIT>(a, *sg, cfg, num_sms, stream, info)
-                         : launch_seg_t<Op, false, true, UNIT>(a, *sg, cfg, num_sms, stream, info);
-    return inclusive ? launch_seg_t<Op, true, false, UNIT>(a, none, cfg, num_sms, stream, info)
-                     : launch_seg_t<Op, false, false, UNIT>(a, none, cfg, num_sms, stream, info);
+        return inclusive ? launch_seg_t<Op, true, true, UNIT, SPLIT>(a, *sg, cfg, num_sms, stream, info)
+                         : launch_seg_t<Op, false, true, UNIT, SPLIT>(a, *sg, cfg, num_sms, stream, info);
+    return inclusive ? launch_seg_t<Op, true, false, UNIT, SPLIT>(a, none, cfg, num_sms, stream, info)
+                     : launch_seg_t<Op, false, false, UNIT, SPLIT>(a, none, cfg, num_sms, stream, info);
 }
 
-template <class Op>
+// The kernels of one scan operation and one row split (threads per row).
+template <class Op, int SPLIT>
 cudaError_t launch_seg_op(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg, int num_sms,
                           cudaStream_t stream, LaunchInfo* info) {
+    if (cfg.split != static_cast<uint32_t>(SPLIT)) return cudaErrorInvalidValue;
     switch (cfg.unit) {
-        case 1: return launch_seg_unit<Op, 1>(inclusive, a, sg, cfg, num_sms, stream, info);
-        case 4: return launch_seg_unit<Op, 4>(inclusive, a, sg, cfg, num_sms, stream, info);
+        case 1: return launch_seg_unit<Op, 1, SPLIT>(inclusive, a, sg, cfg, num_sms, stream, info);
+        case 4: return launch_seg_unit<Op, 4, SPLIT>(inclusive, a, sg, cfg, num_sms, stream, info);
     }
     return cudaErrorInvalidValue;
 }

@@ -4,6 +4,7 @@
 namespace gps {
 cudaError_t launch_seg_u32x4(bool inclusive, const ScanArgs& a, const SegArgs* sg, const GenericConfig& cfg,
                              int num_sms, cudaStream_t stream, LaunchInfo* info) {
-    return launch_seg_op<OpU32x4>(inclusive, a, sg, cfg, num_sms, stream, info);
+    if (cfg.split == 2) return launch_seg_u32x4_x2(inclusive, a, sg, cfg, num_sms, stream, info);
+    return launch_seg_op<OpU32x4, 1>(inclusive, a, sg, cfg, num_sms, stream, info);
 }
 }  // namespace gps

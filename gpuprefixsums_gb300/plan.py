@@ -137,28 +137,31 @@ class Plan:
     def autotune(self, x, offsets=None, out=None, inclusive: bool = False, stream=None) -> dict:
         """Times the generic kernel's launch configurations on these tensors
         (batched when offsets is given) and keeps the fastest for the size
-        class of x.numel(); returns it. Synchronizes; not inside a capture."""
+        class of x.numel(); returns it. out must not be x. Synchronizes; not
+        inside a capture."""
         if out is None:
             import torch
             out = torch.empty_like(x)
         kind = _lib.INCLUSIVE if inclusive else _lib.EXCLUSIVE
-        unit, div = ctypes.c_uint32(), ctypes.c_uint32()
+        unit, div, split = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         off_ptr = ctypes.c_void_p(offsets.data_ptr()) if offsets is not None else ctypes.c_void_p()
         nseg = offsets.numel() - 1 if offsets is not None else 0
         check(lib.gps_plan_autotune(self._h, kind, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
                                     self.length(x), off_ptr, nseg, ctypes.c_void_p(_stream_handle(stream)),
-                                    ctypes.byref(unit), ctypes.byref(div)), "gps_plan_autotune")
-        return {"unit_tiles": unit.value, "ctas_div": div.value}
+                                    ctypes.byref(unit), ctypes.byref(div), ctypes.byref(split)), "gps_plan_autotune")
+        return {"unit_tiles": unit.value, "ctas_div": div.value, "threads_per_row": split.value}
 
     def generic_config(self, n: int, segmented: bool = True) -> dict:
-        unit, div, tuned = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int()
+        unit, div, split, tuned = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int()
         check(lib.gps_plan_generic_config(self._h, int(segmented), int(n), ctypes.byref(unit), ctypes.byref(div),
-                                          ctypes.byref(tuned)), "gps_plan_generic_config")
-        return {"unit_tiles": unit.value, "ctas_div": div.value, "tuned": bool(tuned.value)}
+                                          ctypes.byref(split), ctypes.byref(tuned)), "gps_plan_generic_config")
+        return {"unit_tiles": unit.value, "ctas_div": div.value, "threads_per_row": split.value,
+                "tuned": bool(tuned.value)}
 
-    def set_generic_config(self, n: int, unit_tiles: int, ctas_div: int = 1, segmented: bool = True) -> None:
-        check(lib.gps_plan_set_generic_config(self._h, int(segmented), int(n), int(unit_tiles), int(ctas_div)),
-              "gps_plan_set_generic_config")
+    def set_generic_config(self, n: int, unit_tiles: int, ctas_div: int = 1, segmented: bool = True,
+                           threads_per_row: int = 1) -> None:
+        check(lib.gps_plan_set_generic_config(self._h, int(segmented), int(n), int(unit_tiles), int(ctas_div),
+                                              int(threads_per_row)), "gps_plan_set_generic_config")
 
     def scan_host(self, h_in: int, h_out: int, n: int, inclusive: bool = False, stream=None) -> None:
         """Scan n elements of a host array (pointers; pinned memory for speed)."""

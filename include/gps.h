@@ -150,31 +150,42 @@ gps_status gps_select_flagged(gps_plan plan, const void* d_in, const uint8_t* d_
                               uint64_t* d_num_selected, gps_stream_t stream);
 
 /* Autotuner of the batched / floating-point kernel. Times each launch
- * configuration it knows -- tiles per lookback unit (1 or 4 tiles of 4096
- * 4-byte or 2048 8-byte elements) times CTA count (one per SM, or half) -- on
- * these buffers (same arguments as gps_scan_segmented; d_offsets NULL for a
- * plain scan of a floating-point plan), and keeps the fastest for every later
- * scan of this plan of the same kind (batched or plain) whose n is in the
- * same size class (n within a factor of four). Without tuning a size class
- * uses units of 4 tiles once there are two such units per SM, else 1 tile.
- * d_out is overwritten (with a correct result). Synchronizes `stream`; not
- * allowed while the stream is being captured. The chosen configuration is
- * returned in out_unit / out_ctas_div (either may be NULL).
+ * configuration it knows on these buffers -- tiles per lookback unit (1 or 4
+ * tiles of 4096 4-byte or 2048 8-byte elements) x CTA count (one per SM, or
+ * half) x threads per 128-byte row of a tile (1: each thread scans 128
+ * bytes, 32 four-byte items; 2: twice the threads, 16 items each) -- and keeps
+ * the fastest for every later scan of this plan of the same kind (batched or
+ * plain) whose n is in the same size class (n within a factor of four). The
+ * arguments are those of gps_scan_segmented (d_offsets NULL for a plain scan
+ * of a floating-point or struct plan); d_in and d_out must be separate
+ * buffers. On integer and struct plans every candidate's output is checked
+ * against the first candidate's (a 64-bit hash computed on the device):
+ * a configuration whose result differs is not taken and the call returns
+ * GPS_ERR_CUDA after tuning with the others. A shape that does not fit one
+ * CTA's shared memory for the element type is skipped. Without tuning a
+ * size class uses one thread per row and units of 4 tiles once there are
+ * two such units per SM, else 1 tile. d_out is left holding a correct
+ * result. Synchronizes `stream`; not allowed while the stream is being
+ * captured. The chosen configuration is returned in out_unit /
+ * out_ctas_div / out_threads_per_row (any may be NULL).
  * No counterpart in the reference: its tile shape and grid are compile-time
  * constants (ChainedScanDecoupledLookbackDispatcher.cuh:13-18). */
 gps_status gps_plan_autotune(gps_plan plan, gps_scan_kind kind, const void* d_in, void* d_out, uint64_t n,
                              const uint32_t* d_offsets, uint64_t num_segments, gps_stream_t stream,
-                             uint32_t* out_unit, uint32_t* out_ctas_div);
+                             uint32_t* out_unit, uint32_t* out_ctas_div, uint32_t* out_threads_per_row);
 
 /* Launch configuration a batched (segmented != 0) or plain generic-kernel
  * scan of n elements would use now: tiles per unit, CTA divisor (1: one CTA
- * per SM, 2: half), and whether it comes from gps_plan_autotune(). */
+ * per SM, 2: half), threads per row (1 or 2), and whether it comes from
+ * gps_plan_autotune() or gps_plan_set_generic_config(). */
 gps_status gps_plan_generic_config(gps_plan plan, int segmented, uint64_t n, uint32_t* out_unit,
-                                   uint32_t* out_ctas_div, int* out_tuned);
+                                   uint32_t* out_ctas_div, uint32_t* out_threads_per_row, int* out_tuned);
 
 /* Sets the launch configuration of a size class by hand (to restore a saved
- * tuning, or to test one configuration): unit 1 or 4, ctas_div 1 or 2. */
-gps_status gps_plan_set_generic_config(gps_plan plan, int segmented, uint64_t n, uint32_t unit, uint32_t ctas_div);
+ * tuning, or to test one configuration): unit 1 or 4, ctas_div 1 or 2,
+ * threads_per_row 1 or 2. */
+gps_status gps_plan_set_generic_config(gps_plan plan, int segmented, uint64_t n, uint32_t unit, uint32_t ctas_div,
+                                       uint32_t threads_per_row);
 
 /* Scan of a host array: copies h_in to the device, scans, copies the result
  * to h_out, in chunks so that the copies in both directions overlap the

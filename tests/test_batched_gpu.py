@@ -142,8 +142,9 @@ def test_segmented_and_plain_scans_share_a_u32_plan(cuda, max_n):
             assert np.array_equal(full.cpu().numpy().view(np.uint32), want)
 
 
+@pytest.mark.parametrize("split", [1, 2])
 @pytest.mark.parametrize("unit,ctas_div", [(1, 1), (4, 1), (1, 2), (4, 2)])
-def test_every_launch_configuration_is_exact(cuda, unit, ctas_div):
+def test_every_launch_configuration_is_exact(cuda, unit, ctas_div, split):
     lengths = config3_lengths(seed=11)[:600]
     offs = offsets_of(lengths)
     n = int(offs[-1])
@@ -152,9 +153,10 @@ def test_every_launch_configuration_is_exact(cuda, unit, ctas_div):
     d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
     xf = fp_input("normal", n, seed=5)
     with Plan("csdl", "u32", max_n=n) as plan, Plan("csdl", "f32c", max_n=n) as fplan:
-        plan.set_generic_config(n, unit, ctas_div)
-        fplan.set_generic_config(n, unit, ctas_div, segmented=False)
-        assert plan.generic_config(n) == {"unit_tiles": unit, "ctas_div": ctas_div, "tuned": True}
+        plan.set_generic_config(n, unit, ctas_div, threads_per_row=split)
+        fplan.set_generic_config(n, unit, ctas_div, segmented=False, threads_per_row=split)
+        assert plan.generic_config(n) == {"unit_tiles": unit, "ctas_div": ctas_div, "threads_per_row": split,
+                                          "tuned": True}
         for inclusive in (False, True):
             got = plan.scan_segmented(dev(x), d_off, inclusive=inclusive)
             plan.check()
@@ -175,7 +177,7 @@ def test_autotune_keeps_a_configuration_per_size_class(cuda):
         assert not plan.generic_config(n)["tuned"]
         choice = plan.autotune(dev(x), d_off)
         cfg = plan.generic_config(n)
-        assert cfg["tuned"] and (cfg["unit_tiles"], cfg["ctas_div"]) == (choice["unit_tiles"], choice["ctas_div"])
+        assert cfg["tuned"] and {k: cfg[k] for k in choice} == choice
         assert not plan.generic_config(n // 16)["tuned"]  # another size class
         got = plan.scan_segmented(dev(x), d_off)
         plan.check()

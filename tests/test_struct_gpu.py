@@ -78,12 +78,20 @@ def test_segmented_struct_scan(cuda, inclusive):
     assert np.array_equal(host(got), oracle.scan_members(x, offs, inclusive))
 
 
+@pytest.mark.parametrize("split", [1, 2])
 @pytest.mark.parametrize("unit,ctas_div", [(1, 1), (4, 1), (1, 2), (4, 2)])
-def test_every_launch_configuration_is_exact(cuda, unit, ctas_div):
+def test_every_launch_configuration_is_exact(cuda, unit, ctas_div, split):
     n = 3_000_001
-    x = random_structs(n, seed=unit + 7 * ctas_div)
+    x = random_structs(n, seed=unit + 7 * ctas_div + 13 * split)
     with Plan("csdl", "u32x4", max_n=n) as plan:
-        plan.set_generic_config(n, unit, ctas_div, segmented=False)
+        if split == 2 and unit == 4:
+            # Two threads per row of 16-byte structs with 4-tile units need
+            # more shared memory than one CTA has.
+            with pytest.raises(GpsError) as e:
+                plan.set_generic_config(n, unit, ctas_div, segmented=False, threads_per_row=split)
+            assert e.value.status == GPS_ERR_UNSUPPORTED
+            return
+        plan.set_generic_config(n, unit, ctas_div, segmented=False, threads_per_row=split)
         got = plan.scan(dev(x), inclusive=False)
         plan.check()
     assert np.array_equal(host(got), oracle.scan_members(x, inclusive=False))
