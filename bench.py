@@ -751,8 +751,24 @@ def run_ours(args, world, rank, local):
             plan.scan_host(h_in.data_ptr(), h_out.data_ptr(), n, stream=stream)
         e2e_s = (time.perf_counter() - te) / args.e2e_steps
         e2e_s = max_over_ranks(e2e_s, dist)
+        # The copies alone, one direction at a time, over the same bytes: with
+        # the chunks fully overlapped the end-to-end step approaches the
+        # slower direction, serialised it approaches their sum.
+        def copy_ms(fn):
+            fn()
+            torch.cuda.synchronize()
+            tc = time.perf_counter()
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            return (time.perf_counter() - tc) / 3 * 1e3
+        h2d_ms = copy_ms(lambda: d_out.copy_(h_in, non_blocking=True))
+        d2h_ms = copy_ms(lambda: h_out.copy_(d_in, non_blocking=True))
+        e2e_ms = e2e_s * 1e3
         e2e = {"value": round(world * alg_bytes / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": n * 4,
-               "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_s * 1e3, 3),
+               "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_ms, 3),
+               "h2d_only_ms": round(h2d_ms, 3), "d2h_only_ms": round(d2h_ms, 3),
+               "overlap_of_copies": round(max(0.0, min(1.0, (h2d_ms + d2h_ms - e2e_ms) / min(h2d_ms, d2h_ms))), 3),
                "path": "gps_scan_host: pinned host -> device -> host, chunked and overlapped"}
 
         if not args.no_extras:

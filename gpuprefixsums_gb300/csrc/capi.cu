@@ -29,6 +29,15 @@ inline int size_class(uint64_t n) {
     return std::min(kSizeClasses - 1, bits / 2);
 }
 
+// Staging buffers of gps_scan_host, and their size in bytes (at most): four
+// chunks of 16 MB keep copies in both directions and the scans going at once.
+// Measured on GB300 with 1 GiB each way (pinned): either direction alone
+// takes 5.09 / 5.56 ms, both at once 6.28 ms (the host link does not carry
+// both at full rate). The scan of the array takes 7.01 ms with four 16 MB
+// chunks, 7.16 ms with two of 64 MB.
+constexpr int kHostStages = 4;
+constexpr uint64_t kHostChunkBytes = 16ull << 20;
+
 struct gps_plan_s {
     gps_algo algo;
     gps_dtype dtype;
@@ -62,10 +71,10 @@ struct gps_plan_s {
     gps::StallConfig stall;
     gps::LaunchInfo last_launch;
     // Staging for gps_scan_host, created on first use.
-    void* stage[2];
+    void* stage[kHostStages];
     uint64_t stage_elems;
     cudaStream_t copy_in, compute, copy_out;
-    cudaEvent_t ev_loaded[2], ev_scanned[2], ev_free[2], ev_start, ev_done;
+    cudaEvent_t ev_loaded[kHostStages], ev_scanned[kHostStages], ev_free[kHostStages], ev_start, ev_done;
 };
 
 namespace {
@@ -335,7 +344,7 @@ gps_status gps_plan_destroy(gps_plan p) {
     cudaGetDevice(&prev);
     cudaSetDevice(p->device);
     cudaError_t err = cudaFree(p->scratch);
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kHostStages; ++b) {
         if (p->stage[b]) cudaFree(p->stage[b]);
         if (p->ev_loaded[b]) cudaEventDestroy(p->ev_loaded[b]);
         if (p->ev_scanned[b]) cudaEventDestroy(p->ev_scanned[b]);
@@ -607,14 +616,14 @@ gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void*
     const size_t es = gps::dtype_size(p->dtype);
     cudaError_t err = cudaSuccess;
     if (p->stage[0] == nullptr) {
-        // Chunk: up to 2^24 elements, whole tiles, within the plan's size.
-        uint64_t chunk = std::min<uint64_t>(p->max_n, 1ull << 24);
+        // Chunk: up to 16 MB, whole tiles, within the plan's size.
+        uint64_t chunk = std::min<uint64_t>(p->max_n, kHostChunkBytes / es);
         if (chunk > p->tile_elems) chunk -= chunk % p->tile_elems;
-        for (int b = 0; b < 2 && err == cudaSuccess; ++b) err = cudaMalloc(&p->stage[b], chunk * es);
+        for (int b = 0; b < kHostStages && err == cudaSuccess; ++b) err = cudaMalloc(&p->stage[b], chunk * es);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->copy_in, cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->compute, cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->copy_out, cudaStreamNonBlocking);
-        for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+        for (int b = 0; b < kHostStages && err == cudaSuccess; ++b) {
             err = cudaEventCreateWithFlags(&p->ev_loaded[b], cudaEventDisableTiming);
             if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_scanned[b], cudaEventDisableTiming);
             if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_free[b], cudaEventDisableTiming);
@@ -632,10 +641,10 @@ gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void*
     if (err == cudaSuccess) err = cudaStreamWaitEvent(p->copy_in, p->ev_start, 0);
     const uint64_t chunks = (n + p->stage_elems - 1) / p->stage_elems;
     for (uint64_t k = 0; k < chunks && err == cudaSuccess; ++k) {
-        const int b = static_cast<int>(k & 1);
+        const int b = static_cast<int>(k % kHostStages);
         const uint64_t off = k * p->stage_elems;
         const uint64_t cnt = std::min<uint64_t>(p->stage_elems, n - off);
-        if (k >= 2) err = cudaStreamWaitEvent(p->copy_in, p->ev_free[b], 0);
+        if (k >= kHostStages) err = cudaStreamWaitEvent(p->copy_in, p->ev_free[b], 0);
         if (err == cudaSuccess)
             err = cudaMemcpyAsync(p->stage[b], static_cast<const char*>(h_in) + off * es, cnt * es,
                                   cudaMemcpyHostToDevice, p->copy_in);
