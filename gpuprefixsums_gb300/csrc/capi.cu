@@ -57,6 +57,11 @@ struct gps_plan_s {
     // u32 kernel; on other plans they are hdr and area.
     gps::WsHeader* hdr16;
     void* desc16;
+    // Group descriptors of the generic kernel's deterministic mode, in the
+    // same region after the unit descriptors (so that the epoch-wrap clear
+    // covers them), and whether the mode is on.
+    void* group_desc16;
+    int deterministic;
     // Integer chained-scan plans: the 16-byte, launch-tagged descriptors of
     // the one-tile-per-CTA kernels (mid.cu), one per tile; else null.
     void* desc_mid;
@@ -174,6 +179,8 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
     if (generic_only(p->dtype)) {
         a.hdr = p->hdr16;
         a.desc = p->desc16;
+        a.group_desc = p->group_desc16;
+        a.deterministic = p->deterministic ? 1u : 0u;
         err = launch_generic(p->dtype, inclusive, a, nullptr, generic_config(p, false, n), p->num_sms, stream,
                              &p->last_launch);
     } else if (n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
@@ -288,12 +295,17 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     }
     // Chained scan: one descriptor per tile plus the lookback padding;
     // reduce-then-scan: one tile sum per tile.
+    // Generic-kernel descriptors are followed by the group descriptors of its
+    // deterministic mode (one per 128 lookback units of one tile).
     const size_t per_tile = algo == GPS_ALGO_CSDL ? desc_bytes(dtype) : gps::dtype_size(dtype);
-    const uint64_t slots = algo == GPS_ALGO_CSDL ? tiles + gps::kDescPad : tiles;
+    const uint64_t det_groups = gps::det_group_slots(tiles);
+    const uint64_t slots =
+        algo == GPS_ALGO_CSDL ? tiles + gps::kDescPad + (dtype != GPS_DTYPE_U32 ? det_groups : 0) : tiles;
     // u32 chained-scan plans keep 8-byte descriptors; batched scans of them
     // use the generic kernel's 16-byte descriptors, kept in a region of their
     // own so that the two formats never meet in one slot.
-    const uint64_t slots16 = (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? tiles + gps::kDescPad : 0;
+    const uint64_t slots16 =
+        (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? tiles + gps::kDescPad + det_groups : 0;
     // One-tile-per-CTA kernels of integer chained-scan plans: 16-byte
     // descriptors tagged with the launch, in a region no other kernel uses.
     const uint64_t slots_mid = (algo == GPS_ALGO_CSDL && !generic_only(dtype)) ? tiles + gps::kDescPad : 0;
@@ -317,6 +329,8 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
     p->hdr16 = slots16 ? reinterpret_cast<gps::WsHeader*>(static_cast<char*>(p->scratch) + region16) : p->hdr;
     p->desc16 = slots16 ? static_cast<char*>(p->scratch) + region16 + kHeaderBytes : p->area;
+    if (algo == GPS_ALGO_CSDL)
+        p->group_desc16 = static_cast<char*>(p->desc16) + (tiles + gps::kDescPad) * (slots16 ? 16 : per_tile);
     p->desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid : nullptr;
     p->group_desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid + slots_mid * 16 : nullptr;
     gps::WsHeader h{};
@@ -430,6 +444,8 @@ gps_status prepare_generic(gps_plan_s* p, gps_scan_kind kind, const void* d_in, 
     a->num_tiles = static_cast<uint32_t>((n + p->tile_elems - 1) / p->tile_elems);
     a->hdr = p->hdr16;
     a->desc = p->desc16;
+    a->group_desc = p->group_desc16;
+    a->deterministic = p->deterministic ? 1u : 0u;
     a->wait_budget_ns = p->wait_budget_ns;
     *sg = gps::SegArgs{d_offsets, static_cast<uint32_t>(num_segments)};
     return GPS_OK;
@@ -736,6 +752,14 @@ gps_status gps_plan_geometry(gps_plan p, uint64_t n, uint32_t* tile_elems, uint3
     if (grid) *grid = static_cast<uint32_t>(p->last_launch.grid);
     const bool small = !generic_only(p->dtype) && n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0;
     if (launches) *launches = n == 0 ? 0u : (small || p->algo == GPS_ALGO_CSDL ? 1u : 3u);
+    return GPS_OK;
+}
+
+gps_status gps_plan_set_deterministic(gps_plan p, int on) {
+    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (on && p->algo != GPS_ALGO_CSDL)
+        return fail(GPS_ERR_UNSUPPORTED, "the deterministic mode applies to the generic chained scan only");
+    p->deterministic = on ? 1 : 0;
     return GPS_OK;
 }
 

@@ -68,15 +68,23 @@ struct StallConfig {
 
 enum class PrefixMode : int { Lookback = 0, Spine = 1 };
 
+// Deterministic mode of the generic kernel: lookback units per group, and the
+// group descriptors a plan keeps for up to `units` units (one more than the
+// groups, as slack for the last partial group).
+constexpr uint32_t kDetGroupUnits = 128;
+constexpr uint64_t det_group_slots(uint64_t units) { return (units + kDetGroupUnits - 1) / kDetGroupUnits + 1; }
+
 struct ScanArgs {
     const void* in;
     void* out;
     uint64_t n;
     uint32_t num_tiles;
-    uint32_t pad_;
+    uint32_t deterministic;  // generic kernel: prefixes summed in a fixed order
     WsHeader* hdr;       // plan state (counters, epoch, error flags)
     void* desc;          // tile descriptors (lookback)
-    void* group_desc;    // one-tile-per-CTA kernels: descriptors of groups of 32 tiles
+    // Descriptors of groups: of 32 tiles for the one-tile-per-CTA kernels, of
+    // 128 lookback units for the generic kernel's deterministic mode.
+    void* group_desc;
     const void* spine;   // inclusive scan of tile sums (reduce-then-scan)
     const void* carry_in;  // optional: one element added to every output
     void* carry_out;       // optional: receives carry_in + sum of all n inputs

@@ -224,6 +224,107 @@ __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t e
     }
 }
 
+// ------------------------------------------------------ deterministic mode
+// The lookback above sums whichever predecessors' descriptors it finds ready,
+// so a floating-point prefix depends on timing. In deterministic mode the
+// units form groups of kDetGroupUnits, units keep their aggregate in their
+// descriptor (they never publish an inclusive prefix there), and the prefix
+// of unit u in group g is
+//     P(g) + fold(aggregates of units 128g .. u-1),
+// where the fold has a fixed shape (each lane folds its 4 consecutive units
+// in order, then an order-keeping butterfly over the lanes) and P(g), the
+// prefix before group g, is a chain: the last unit of each group publishes
+// P(g + 1) = prefix + aggregate in the group descriptor array, as an
+// inclusive value. Every addition then has fixed operands in a fixed order.
+// The group prefixes pass from group to group one at a time (one L2 round
+// trip per 128 units). Segment heads fold in the same fixed order, and a
+// head among the in-group predecessors makes P(g) unnecessary.
+static_assert(kDetGroupUnits == 128, "the fold gives each lane 4 units");
+
+template <class Op>
+__device__ typename Op::C seg_lookback_det(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane) {
+    using C = typename Op::C;
+    constexpr int K = static_cast<int>(kDetGroupUnits / 32);
+    const ptx::u64x2* desc = static_cast<const ptx::u64x2*>(a.desc);
+    const ptx::u64x2* gdesc = static_cast<const ptx::u64x2*>(a.group_desc);
+    const uint32_t g = u / kDetGroupUnits;
+    const uint32_t i0 = g * kDetGroupUnits;
+    const uint32_t cnt = u - i0;  // in-group predecessors
+    C v[K];
+    bool f[K];
+    uint32_t ready = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        v[j] = Op::chain_zero();
+        f[j] = false;
+        if (lane * K + j >= cnt) ready |= 1u << j;  // not a predecessor: identity
+    }
+    uint32_t polls = 0, backoff = 64;
+    uint64_t deadline = 0;
+    auto expired = [&]() -> bool {
+        ++polls;
+        if ((polls & 15u) == 1u) {
+            const uint64_t now = ptx::global_timer_ns();
+            if (deadline == 0) deadline = now + a.wait_budget_ns;
+            bool give_up = now > deadline || ld_volatile_u32(&a.hdr->error_flags) != 0;
+            give_up = __shfl_sync(kFullMask, give_up, 0);
+            if (give_up) {
+                if (lane == 0) raise_error(a.hdr, kErrLookbackTimeout);
+                return true;
+            }
+        }
+        __nanosleep(backoff);
+        backoff = backoff < 1024 ? backoff * 2 : 1024;
+        return false;
+    };
+    // 1. The in-group aggregates.
+    while (true) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            if (!((ready >> j) & 1u)) {
+                bool hf = false;
+                C cv;
+                if (desc_load<Op>(desc, i0 + lane * K + j, epoch, hf, cv) != kNotReady) {
+                    v[j] = cv;
+                    f[j] = hf;
+                    ready |= 1u << j;
+                }
+            }
+        }
+        if (__all_sync(kFullMask, ready == (1u << K) - 1u)) break;
+        if (expired()) return Op::chain_zero();
+    }
+    // 2. Their fold in a fixed shape, in unit order.
+    C c = v[0];
+    bool fl = f[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) {
+        c = f[j] ? v[j] : Op::chain_add(c, v[j]);
+        fl = fl || f[j];
+    }
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        const C oc = Op::chain_shfl_xor(c, m);
+        const bool of = __shfl_xor_sync(kFullMask, fl, m) != 0;
+        if (lane & static_cast<uint32_t>(m))
+            c = fl ? c : Op::chain_add(oc, c);  // the partner holds the block on the left
+        else
+            c = of ? oc : Op::chain_add(c, oc);
+        fl = fl || of;
+    }
+    if (fl || g == 0) return c;
+    // 3. The group prefix (every lane reads the one descriptor; it is
+    // written once per launch, so all lanes that see it see the same value).
+    C gp = Op::chain_zero();
+    while (true) {
+        bool hf = false;
+        const bool ok = desc_load<Op>(gdesc, g - 1, epoch, hf, gp) == kInclusive;
+        if (__all_sync(kFullMask, ok)) break;
+        if (expired()) return Op::chain_zero();
+    }
+    return Op::chain_add(gp, c);
+}
+
 template <class Op, int RW, int RS, int SS, int Q, int G, bool SEG>
 struct SegCtrl {
     using S = typename Op::S;
@@ -679,7 +780,9 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             }
             const uint32_t u = ctrl->unit_of[q];
             if (u == kTileEnd) break;
-            const C pre = u == 0 ? Op::chain_zero() : seg_lookback<Op>(a, u, epoch, lane, own_prev, own_incl);
+            const C pre = u == 0         ? Op::chain_zero()
+                          : a.deterministic ? seg_lookback_det<Op>(a, u, epoch, lane)
+                                            : seg_lookback<Op>(a, u, epoch, lane, own_prev, own_incl);
             uint32_t state = 0;
             if (lane == 0) {
                 const uint64_t deadline = ptx::global_timer_ns() + long_budget;
@@ -704,7 +807,15 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             const bool flag = ctrl->uflag[q] != 0;
             const C incl = flag ? agg : Op::chain_add(pre, agg);
             if (lane == 0) {
-                if (u != 0) desc_store<Op>(desc, u, kInclusive, flag, epoch, incl);
+                if (a.deterministic) {
+                    // Descriptors keep the aggregate; the last unit of a
+                    // group passes the group prefix on.
+                    if ((u % kDetGroupUnits) == kDetGroupUnits - 1)
+                        desc_store<Op>(static_cast<ptx::u64x2*>(a.group_desc), u / kDetGroupUnits, kInclusive, false,
+                                       epoch, incl);
+                } else if (u != 0) {
+                    desc_store<Op>(desc, u, kInclusive, flag, epoch, incl);
+                }
                 ctrl->upre[q] = pre;
                 ptx::mbar_arrive(&ctrl->uprefix[q]);
             }

@@ -233,6 +233,18 @@ gps_status gps_plan_set_stall(gps_plan plan, uint32_t mode, uint32_t period, uin
  * which the CUDA part only shows in its EmulatedDeadlocking test. */
 gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
 
+/* Deterministic mode of the generic kernel (floating-point and struct
+ * scans, and every batched scan) on a GPS_ALGO_CSDL plan; off by default.
+ * By default a lookback sums whichever predecessors' descriptors it finds
+ * published, so the rounding of a floating-point result can change from one
+ * run to the next. With the mode on, every prefix is summed in a fixed order
+ * -- a fixed-shape fold of the preceding units of its group of 128 lookback
+ * units, after the chained prefix of the groups before it -- so two runs
+ * with the same inputs and launch configuration (gps_plan_generic_config)
+ * give bitwise-identical outputs. Integer results are exact either way.
+ * No counterpart in the reference, whose scans are integer only. */
+gps_status gps_plan_set_deterministic(gps_plan plan, int on);
+
 /* Integer scans of at most max_n elements (maximum: 64 KB of input, 16384
  * u32 or 8192 u64) run in a single CTA instead of the multi-CTA kernels.
  * Default: 64 KB on GPS_ALGO_RTS plans; 0 on GPS_ALGO_CSDL plans, whose
