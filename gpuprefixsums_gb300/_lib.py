@@ -62,7 +62,6 @@ SIGNATURES = [
     ("gps_plan_set_fallback", _INT, [_P, _U32]),
     ("gps_plan_set_small_max", _INT, [_P, _U64]),
     ("gps_plan_set_mid_max", _INT, [_P, _U64]),
-    ("gps_plan_set_deterministic", _INT, [_P, _INT]),
     ("gps_plan_stats", _INT, [_P, _P, ctypes.POINTER(LookbackStats)]),
     ("gps_plan_geometry", _INT, [_P, _U64, ctypes.POINTER(_U32), ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
     ("gps_scan_u32_noalloc", _INT, [_INT, _P, _P, _U64, _P]),

@@ -57,11 +57,10 @@ struct gps_plan_s {
     // u32 kernel; on other plans they are hdr and area.
     gps::WsHeader* hdr16;
     void* desc16;
-    // Group descriptors of the generic kernel's deterministic mode, in the
+    // Group descriptors of the generic kernel's fixed-order lookback, in the
     // same region after the unit descriptors (so that the epoch-wrap clear
-    // covers them), and whether the mode is on.
+    // covers them).
     void* group_desc16;
-    int deterministic;
     // Integer chained-scan plans: the 16-byte, launch-tagged descriptors of
     // the one-tile-per-CTA kernels (mid.cu), one per tile; else null.
     void* desc_mid;
@@ -180,7 +179,6 @@ gps_status launch_scan(gps_plan_s* p, bool inclusive, const void* in, void* out,
         a.hdr = p->hdr16;
         a.desc = p->desc16;
         a.group_desc = p->group_desc16;
-        a.deterministic = p->deterministic ? 1u : 0u;
         err = launch_generic(p->dtype, inclusive, a, nullptr, generic_config(p, false, n), p->num_sms, stream,
                              &p->last_launch);
     } else if (n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0) {
@@ -296,7 +294,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     // Chained scan: one descriptor per tile plus the lookback padding;
     // reduce-then-scan: one tile sum per tile.
     // Generic-kernel descriptors are followed by the group descriptors of its
-    // deterministic mode (one per 128 lookback units of one tile).
+    // lookback (one per kDetGroupUnits single-tile units, and a spare).
     const size_t per_tile = algo == GPS_ALGO_CSDL ? desc_bytes(dtype) : gps::dtype_size(dtype);
     const uint64_t det_groups = gps::det_group_slots(tiles);
     const uint64_t slots =
@@ -435,7 +433,7 @@ gps_status prepare_generic(gps_plan_s* p, gps_scan_kind kind, const void* d_in, 
         return fail(GPS_ERR_INVALID_ARGUMENT, "input and output overlap without being identical");
     gps_status st = check_device(p);
     if (st != GPS_OK) return st;
-    if ((reinterpret_cast<uintptr_t>(p->desc16) & 15u) != 0)
+    if (((reinterpret_cast<uintptr_t>(p->desc16) | reinterpret_cast<uintptr_t>(p->group_desc16)) & 15u) != 0)
         return fail(GPS_ERR_CUDA, "internal: misaligned descriptor region");
     *a = gps::ScanArgs{};
     a->in = d_in;
@@ -445,7 +443,6 @@ gps_status prepare_generic(gps_plan_s* p, gps_scan_kind kind, const void* d_in, 
     a->hdr = p->hdr16;
     a->desc = p->desc16;
     a->group_desc = p->group_desc16;
-    a->deterministic = p->deterministic ? 1u : 0u;
     a->wait_budget_ns = p->wait_budget_ns;
     *sg = gps::SegArgs{d_offsets, static_cast<uint32_t>(num_segments)};
     return GPS_OK;
@@ -752,14 +749,6 @@ gps_status gps_plan_geometry(gps_plan p, uint64_t n, uint32_t* tile_elems, uint3
     if (grid) *grid = static_cast<uint32_t>(p->last_launch.grid);
     const bool small = !generic_only(p->dtype) && n <= p->small_max && p->stall.mode == 0 && p->stall.fallback_polls == 0;
     if (launches) *launches = n == 0 ? 0u : (small || p->algo == GPS_ALGO_CSDL ? 1u : 3u);
-    return GPS_OK;
-}
-
-gps_status gps_plan_set_deterministic(gps_plan p, int on) {
-    if (p == nullptr) return fail(GPS_ERR_INVALID_ARGUMENT, "plan is NULL");
-    if (on && p->algo != GPS_ALGO_CSDL)
-        return fail(GPS_ERR_UNSUPPORTED, "the deterministic mode applies to the generic chained scan only");
-    p->deterministic = on ? 1 : 0;
     return GPS_OK;
 }
 

@@ -68,9 +68,9 @@ struct StallConfig {
 
 enum class PrefixMode : int { Lookback = 0, Spine = 1 };
 
-// Deterministic mode of the generic kernel: lookback units per group, and the
-// group descriptors a plan keeps for up to `units` units (one more than the
-// groups, as slack for the last partial group).
+// Fixed-order lookback of the generic kernel (scan_seg.cuh): lookback units
+// per group, and the group descriptors a plan keeps for up to `units` units
+// (one more than the groups, as slack).
 constexpr uint32_t kDetGroupUnits = 128;
 constexpr uint64_t det_group_slots(uint64_t units) { return (units + kDetGroupUnits - 1) / kDetGroupUnits + 1; }
 
@@ -79,11 +79,11 @@ struct ScanArgs {
     void* out;
     uint64_t n;
     uint32_t num_tiles;
-    uint32_t deterministic;  // generic kernel: prefixes summed in a fixed order
+    uint32_t pad_;
     WsHeader* hdr;       // plan state (counters, epoch, error flags)
     void* desc;          // tile descriptors (lookback)
     // Descriptors of groups: of 32 tiles for the one-tile-per-CTA kernels, of
-    // 128 lookback units for the generic kernel's deterministic mode.
+    // kDetGroupUnits lookback units for the generic kernel.
     void* group_desc;
     const void* spine;   // inclusive scan of tile sums (reduce-then-scan)
     const void* carry_in;  // optional: one element added to every output

@@ -136,115 +136,37 @@ __device__ __forceinline__ uint32_t desc_load(const ptx::u64x2* desc, uint64_t u
     return st;
 }
 
-// Lookback over the generic descriptors (see lookback() in
-// scan_pipeline.cuh for the scheme): terminators are inclusive prefixes and
-// units holding a segment head. Returns the chain value before unit u.
-template <class Op>
-__device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane, int64_t bound,
-                                       typename Op::C bound_val) {
-    using C = typename Op::C;
-    constexpr int K = 8 / Op::kDescWords;  // descriptors per lane per window
-    constexpr int WIN = 32 * K;
-    constexpr uint32_t kNone = 0xFFFFFFFFu;
-    const ptx::u64x2* desc = static_cast<const ptx::u64x2*>(a.desc);
-    C prefix = Op::chain_zero();
-    int64_t top = static_cast<int64_t>(u) - 1;
-    uint32_t polls = 0;
-    uint64_t deadline = 0;
-    uint32_t backoff = 64;
-    while (true) {
-        const int64_t lo = top - WIN + 1;
-        auto slot_idx = [&](int j) -> int64_t { return lo + static_cast<int64_t>(j) * 32 + lane; };
-        C val[K];
-        uint32_t valid = 0, term = 0, pending = 0;
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            const int64_t idx = slot_idx(j);
-            val[j] = Op::chain_zero();
-            if (idx <= bound) {
-                valid |= 1u << j;
-                term |= 1u << j;
-                if (idx == bound) val[j] = bound_val;
-            } else {
-                pending |= 1u << j;
-            }
-        }
-        while (true) {
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                if ((pending >> j) & 1u) {
-                    bool hf = false;
-                    C cv;
-                    const uint32_t st = desc_load<Op>(desc, static_cast<uint64_t>(slot_idx(j)), epoch, hf, cv);
-                    if (st != kNotReady) {
-                        valid |= 1u << j;
-                        pending &= ~(1u << j);
-                        val[j] = cv;
-                        if (st == kInclusive || hf) term |= 1u << j;
-                    }
-                }
-            }
-            uint32_t my_term = kNone;
-#pragma unroll
-            for (int j = 0; j < K; ++j)
-                if ((term >> j) & 1u) my_term = min(my_term, static_cast<uint32_t>(top - slot_idx(j)));
-            const uint32_t pterm = __reduce_min_sync(kFullMask, my_term);
-            uint32_t my_gap = kNone;
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                const uint32_t pos = static_cast<uint32_t>(top - slot_idx(j));
-                if (!((valid >> j) & 1u) && pos < pterm) my_gap = min(my_gap, pos);
-            }
-            const uint32_t gap = __reduce_min_sync(kFullMask, my_gap);
-            if (gap == kNone) {
-                C part = Op::chain_zero();
-#pragma unroll
-                for (int j = 0; j < K; ++j)
-                    if (static_cast<uint32_t>(top - slot_idx(j)) <= pterm) part = Op::chain_add(part, val[j]);
-                prefix = Op::chain_add(prefix, chain_warp_sum<Op>(part));
-                if (pterm != kNone) return prefix;
-                top -= WIN;
-                polls = 0;
-                break;
-            }
-            ++polls;
-            if ((polls & 15u) == 1u) {
-                const uint64_t now = ptx::global_timer_ns();
-                if (deadline == 0) deadline = now + a.wait_budget_ns;
-                bool give_up = now > deadline || ld_volatile_u32(&a.hdr->error_flags) != 0;
-                give_up = __shfl_sync(kFullMask, give_up, 0);
-                if (give_up) {
-                    if (lane == 0) raise_error(a.hdr, kErrLookbackTimeout);
-                    return prefix;
-                }
-            }
-            __nanosleep(backoff);
-            backoff = backoff < 1024 ? backoff * 2 : 1024;
-        }
-    }
-}
-
-// ------------------------------------------------------ deterministic mode
-// The lookback above sums whichever predecessors' descriptors it finds ready,
-// so a floating-point prefix depends on timing. In deterministic mode the
-// units form groups of kDetGroupUnits, units keep their aggregate in their
-// descriptor (they never publish an inclusive prefix there), and the prefix
-// of unit u in group g is
-//     P(g) + fold(aggregates of units 128g .. u-1),
-// where the fold has a fixed shape (each lane folds its 4 consecutive units
-// in order, then an order-keeping butterfly over the lanes) and P(g), the
-// prefix before group g, is a chain: the last unit of each group publishes
-// P(g + 1) = prefix + aggregate in the group descriptor array, as an
-// inclusive value. Every addition then has fixed operands in a fixed order.
-// The group prefixes pass from group to group one at a time (one L2 round
-// trip per 128 units). Segment heads fold in the same fixed order, and a
-// head among the in-group predecessors makes P(g) unnecessary.
-static_assert(kDetGroupUnits == 128, "the fold gives each lane 4 units");
+// Lookback of the generic kernel, in a fixed order. A decoupled lookback
+// that sums whichever predecessors' descriptors it finds ready makes the
+// rounding of a floating-point prefix depend on timing; here the units form
+// groups of G = kDetGroupUnits, a unit's descriptor holds its aggregate only
+// (it is never upgraded to an inclusive prefix), and the prefix of unit u in
+// group g is
+//     P(g) + fold(aggregates of units G*g .. u-1),
+// where the fold has a fixed shape (each lane folds its G/32 consecutive
+// units in order, then an order-keeping butterfly over the lanes) and P(g),
+// the prefix before group g, is a chain: the last unit of each group
+// publishes P(g + 1) = prefix + aggregate in the group descriptor array, as
+// an inclusive value. Every addition has fixed operands in a fixed order, so
+// a launch configuration gives bitwise-identical results from run to run.
+// Segment heads fold in the same order, and a head among the in-group
+// predecessors makes P(g) unnecessary. The group prefixes pass from group to
+// group one at a time, one L2 round trip per G units, which stays off the
+// critical path while G units take longer to stream than that round trip.
+// Measured on GB300 against the lookback that stops at the nearest
+// inclusive prefix (windows of 256 descriptors, back-off up to 1 us): 2^28
+// FP32 in 333 against 342 us, compensated 344 against 355 us, 4096 batched
+// u32 segments (305 M elements) in 381 against 395 us, compensated FP32
+// 506 against 564 us (units of 4 tiles). Groups of 256 units took 348, 357,
+// 390 and 502 us. A back-off of up to 1 us instead of 128 ns while waiting
+// took 338, 349, 380 and 502 us, and 656 against 555 us for 2^28 FP32 in
+// single-tile units, where a group streams in about a microsecond.
+static_assert(kDetGroupUnits % 32 == 0 && kDetGroupUnits <= 32 * 32, "whole lanes of at most 32 units");
 
 template <class Op>
-__device__ typename Op::C seg_lookback_det(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane) {
+__device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane) {
     using C = typename Op::C;
-    constexpr int K = static_cast<int>(kDetGroupUnits / 32);
+    constexpr int K = static_cast<int>(kDetGroupUnits / 32);  // units per lane
     const ptx::u64x2* desc = static_cast<const ptx::u64x2*>(a.desc);
     const ptx::u64x2* gdesc = static_cast<const ptx::u64x2*>(a.group_desc);
     const uint32_t g = u / kDetGroupUnits;
@@ -274,7 +196,7 @@ __device__ typename Op::C seg_lookback_det(const ScanArgs& a, uint32_t u, uint32
             }
         }
         __nanosleep(backoff);
-        backoff = backoff < 1024 ? backoff * 2 : 1024;
+        backoff = backoff < 128 ? backoff * 2 : 128;
         return false;
     };
     // 1. The in-group aggregates.
@@ -764,9 +686,6 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
     }
     // ======================================================== lookback
     else if (warp < kWarpAgg) {
-        ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
-        int64_t own_prev = -1;
-        C own_incl = Op::chain_zero();
         for (uint32_t i = warp - kWarpLookback;; i += LW) {
             const int q = static_cast<int>(i % Q);
             const uint32_t ph = (i / Q) & 1u;
@@ -780,9 +699,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             }
             const uint32_t u = ctrl->unit_of[q];
             if (u == kTileEnd) break;
-            const C pre = u == 0         ? Op::chain_zero()
-                          : a.deterministic ? seg_lookback_det<Op>(a, u, epoch, lane)
-                                            : seg_lookback<Op>(a, u, epoch, lane, own_prev, own_incl);
+            const C pre = u == 0 ? Op::chain_zero() : seg_lookback<Op>(a, u, epoch, lane);
             uint32_t state = 0;
             if (lane == 0) {
                 const uint64_t deadline = ptx::global_timer_ns() + long_budget;
@@ -807,28 +724,21 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             const bool flag = ctrl->uflag[q] != 0;
             const C incl = flag ? agg : Op::chain_add(pre, agg);
             if (lane == 0) {
-                if (a.deterministic) {
-                    // Descriptors keep the aggregate; the last unit of a
-                    // group passes the group prefix on.
-                    if ((u % kDetGroupUnits) == kDetGroupUnits - 1)
-                        desc_store<Op>(static_cast<ptx::u64x2*>(a.group_desc), u / kDetGroupUnits, kInclusive, false,
-                                       epoch, incl);
-                } else if (u != 0) {
-                    desc_store<Op>(desc, u, kInclusive, flag, epoch, incl);
-                }
+                // The last unit of a group passes the group prefix on.
+                if ((u % kDetGroupUnits) == kDetGroupUnits - 1)
+                    desc_store<Op>(static_cast<ptx::u64x2*>(a.group_desc), u / kDetGroupUnits, kInclusive, false,
+                                   epoch, incl);
                 ctrl->upre[q] = pre;
                 ptx::mbar_arrive(&ctrl->uprefix[q]);
             }
-            own_prev = u;
-            own_incl = incl;
             __syncwarp();
         }
     }
     // ======================================================== aggregator
     // Once per unit: scans the unit's thread aggregates (kLaneEntries per
     // lane, a serial chain, then one warp scan of the lane totals),
-    // publishes the unit's aggregate (ureduced: the lookback warp may
-    // publish the inclusive prefix), then leaves each thread's state before
+    // publishes the unit's aggregate (descriptor, and ureduced for the
+    // lookback warp), then leaves each thread's state before
     // it within the unit in place of its aggregate (ustates).
     else if (warp == kWarpAgg) {
         ptx::u64x2* desc = static_cast<ptx::u64x2*>(a.desc);
@@ -874,7 +784,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             if (lane == 0) {
                 const uint32_t u = ctrl->unit_of[q];
                 const C chain = Op::to_chain(Op::norm(unit_agg));
-                desc_store<Op>(desc, u, u == 0 ? kInclusive : kAggregate, unit_flag, epoch, chain);
+                desc_store<Op>(desc, u, kAggregate, unit_flag, epoch, chain);
                 ctrl->uagg[q] = chain;
                 ctrl->uflag[q] = unit_flag;
                 ptx::mbar_arrive(&ctrl->ureduced[q]);

@@ -196,12 +196,6 @@ class Plan:
         persistent kernel above the one-CTA size)."""
         check(lib.gps_plan_set_mid_max(self._h, int(max_n)), "gps_plan_set_mid_max")
 
-    def set_deterministic(self, on: bool = True) -> None:
-        """Generic kernel (floating-point, struct and batched scans): sum
-        every prefix in a fixed order, so that repeated runs with the same
-        launch configuration give bitwise-identical results."""
-        check(lib.gps_plan_set_deterministic(self._h, 1 if on else 0), "gps_plan_set_deterministic")
-
     def stats(self, stream=None) -> dict:
         s = _lib.LookbackStats()
         check(lib.gps_plan_stats(self._h, ctypes.c_void_p(_stream_handle(stream)), ctypes.byref(s)), "gps_plan_stats")

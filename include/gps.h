@@ -55,11 +55,15 @@ typedef enum gps_status {
 typedef enum gps_dtype {
     GPS_DTYPE_U32 = 0, /* uint32_t, sums wrap mod 2^32 (the reference's type) */
     GPS_DTYPE_U64 = 1, /* uint64_t, sums wrap mod 2^64 */
-    /* float, plain FP32 arithmetic throughout (GPS_ALGO_CSDL only) */
+    /* float, plain FP32 arithmetic throughout (GPS_ALGO_CSDL only). The
+     * floating-point scans sum in an order fixed by n, the segments and the
+     * launch configuration (gps_plan_generic_config), never by timing: two
+     * runs with the same inputs and configuration give bitwise-identical
+     * outputs. */
     GPS_DTYPE_F32 = 2,
     /* float in and out; each partial sum carries a TwoSum error term through
      * the thread, warp and block scans, and the value passed between lookback
-     * units is FP64 (GPS_ALGO_CSDL only) */
+     * units is FP64 (GPS_ALGO_CSDL only); repeatable like GPS_DTYPE_F32 */
     GPS_DTYPE_F32_COMPENSATED = 3,
     /* struct of four uint32_t members (16 bytes, e.g. uint4), each member
      * scanned on its own and wrapping mod 2^32 -- the reference's vec4 struct
@@ -232,18 +236,6 @@ gps_status gps_plan_set_stall(gps_plan plan, uint32_t mode, uint32_t period, uin
  * GPUPrefixSumsD3D12/Shaders/ChainedScanDecoupledLookbackDecoupledFallback.hlsl:81-164),
  * which the CUDA part only shows in its EmulatedDeadlocking test. */
 gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
-
-/* Deterministic mode of the generic kernel (floating-point and struct
- * scans, and every batched scan) on a GPS_ALGO_CSDL plan; off by default.
- * By default a lookback sums whichever predecessors' descriptors it finds
- * published, so the rounding of a floating-point result can change from one
- * run to the next. With the mode on, every prefix is summed in a fixed order
- * -- a fixed-shape fold of the preceding units of its group of 128 lookback
- * units, after the chained prefix of the groups before it -- so two runs
- * with the same inputs and launch configuration (gps_plan_generic_config)
- * give bitwise-identical outputs. Integer results are exact either way.
- * No counterpart in the reference, whose scans are integer only. */
-gps_status gps_plan_set_deterministic(gps_plan plan, int on);
 
 /* Integer scans of at most max_n elements (maximum: 64 KB of input, 16384
  * u32 or 8192 u64) run in a single CTA instead of the multi-CTA kernels.

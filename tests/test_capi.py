@@ -76,8 +76,7 @@ def test_plan_create_rejects_bad_arguments_before_any_cuda_call():
 def test_plan_setters_reject_a_null_plan_without_a_gpu():
     from gpuprefixsums_gb300 import _lib, lib
     for call in (lambda: lib.gps_plan_set_small_max(None, 0), lambda: lib.gps_plan_set_mid_max(None, 0),
-                 lambda: lib.gps_plan_set_fallback(None, 0), lambda: lib.gps_plan_set_wait_budget(None, 1000),
-                 lambda: lib.gps_plan_set_deterministic(None, 1)):
+                 lambda: lib.gps_plan_set_fallback(None, 0), lambda: lib.gps_plan_set_wait_budget(None, 1000)):
         assert call() == _lib.GPS_ERR_INVALID_ARGUMENT
         assert b"plan is NULL" in lib.gps_last_error()
 

@@ -1,10 +1,9 @@
-"""Deterministic mode of the generic kernel (gps_plan_set_deterministic):
+"""The generic kernel's lookback sums every prefix in a fixed order:
 repeated floating-point scans with the same inputs and launch configuration
-are bitwise identical, within the same error bounds against the exact prefix
-sums as the default mode (compensated FP32: relative error <= 1e-6; plain
-FP32: normwise error <= 1e-5). Integer batched scans in this mode, whose
-prefixes are folded in the new fixed order with segment heads among them,
-stay bit-exact against the oracle.
+are bitwise identical, and within the error bounds against the exact prefix
+sums (compensated FP32: relative error <= 1e-6; plain FP32: normwise error
+<= 1e-5). Integer batched scans, whose prefixes fold segment heads in that
+order, are bit-exact against the oracle for every launch configuration.
 """
 import numpy as np
 import pytest
@@ -38,7 +37,6 @@ def test_fp_scan_is_bitwise_repeatable(cuda, dt, cfg):
     d = torch.from_numpy(x).cuda()
     exact = oracle.scan_f32_exact(x, inclusive=True)
     with Plan("csdl", dt, max_n=n) as plan:
-        plan.set_deterministic(True)
         plan.set_generic_config(n, unit, ctas_div, segmented=False, threads_per_row=split)
         outs = _repeat(plan, lambda: plan.scan(d, inclusive=True), 4)
     for o in outs[1:]:
@@ -62,7 +60,6 @@ def test_fp_batched_scan_is_bitwise_repeatable(cuda, dt, inclusive):
     d = torch.from_numpy(x).cuda()
     d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
     with Plan("csdl", dt, max_n=n) as plan:
-        plan.set_deterministic(True)
         plan.set_generic_config(n, 1, 1)
         outs = _repeat(plan, lambda: plan.scan_segmented(d, d_off, inclusive=inclusive), 3)
     for o in outs[1:]:
@@ -92,7 +89,6 @@ def test_integer_batched_scan_is_exact(cuda, dtype, cfg):
     x = rng.integers(0, np.iinfo(np_t).max, size=n, dtype=np_t, endpoint=True)
     d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
     with Plan("csdl", dtype, max_n=n) as plan:
-        plan.set_deterministic(True)
         plan.set_generic_config(n, unit, ctas_div, threads_per_row=split)
         for inclusive in (False, True):
             got = plan.scan_segmented(dev(x), d_off, inclusive=inclusive)
@@ -107,8 +103,6 @@ def test_integer_scans_of_changing_sizes_on_one_plan(cuda):
     big = 1 << 23
     x = rng.integers(0, 2 ** 32, size=big, dtype=np.uint64).astype(np.uint32)
     with Plan("csdl", "u32x4", max_n=big // 4) as splan, Plan("csdl", "u32", max_n=big) as plan:
-        plan.set_deterministic(True)
-        splan.set_deterministic(True)
         for n in (big, 4096 * 129 + 5, big - 3, 70_000, big):
             offs = np.array([0, n // 3, n // 3, n], dtype=np.uint64)
             d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
