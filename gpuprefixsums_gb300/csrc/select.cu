@@ -5,16 +5,16 @@
 // non-zero; count goes to *num_selected. The structure is the chained scan's
 // (decoupled lookback over 64-bit counts, as ChainedScanDecoupledLookback.cuh:
 // 79-139 does for sums), with the two passes of scan_l2.cuh:
-//   reduce pass  bulk-load a tile's flags (1 byte per element) with an L2
-//                evict-last policy, count the selected elements of each
-//                thread, leave every thread its count-prefix within the unit
-//                and publish the unit's count;
+//   reduce pass  bulk-load a tile's flags (1 byte per element), turn each
+//                thread's flags into a bit mask, leave every thread its mask
+//                and its count-prefix within the unit in shared memory, and
+//                publish the unit's count;
 //   scan pass    once the previous unit's prefix is known, bulk-load the
-//                tile's values (HBM) and flags (again, from L2), compact each
-//                thread's selected values into a shared-memory staging tile at
-//                their tile-local positions, and copy the staged run out with
-//                coalesced stores at the unit prefix.
-// HBM sees the flags and values once each and only the selected values
+//                tile's values, compact each thread's selected values (by
+//                the reduce pass's mask) into its warp's staging slice at
+//                their warp-local positions, and copy the staged run out with
+//                16-byte stores at the unit prefix.
+// HBM and L2 see the flags and values once each and only the selected values
 // written: (sizeof(V) + 1) bytes read and p * sizeof(V) written per element
 // for a selected fraction p.
 //
@@ -32,7 +32,7 @@ constexpr int kSelRole = kSelWarps * 32;     // threads per role
 constexpr int kSelLookback = 3;
 constexpr int kSelThreads = 32 * (2 + kSelLookback + 2 * kSelWarps);
 constexpr int kSelRS = 8;   // flag stages of the reduce pass
-constexpr int kSelSS = 8;   // value + flag stages of the scan pass
+constexpr int kSelSS = 8;   // value stages of the scan pass
 constexpr int kSelQ = 6;    // units in flight
 constexpr int kSelG = 4;    // tiles per unit
 
@@ -43,6 +43,9 @@ struct SelShape {
     static constexpr int kItems = kTile / kSelRole;  // per thread: 128 bytes of values
     static constexpr int kEpc = 16 / static_cast<int>(sizeof(V));
     static constexpr int kChunks = kItems / kEpc;
+    // A finalize warp's staging slice: its 32 rows, plus one chunk so that a
+    // run can sit at the 16-byte phase of its destination.
+    static constexpr int kSlice = 32 * kItems + kEpc;
 };
 
 template <typename V>
@@ -57,13 +60,15 @@ struct SelCtrl {
     uint64_t uagg[kSelQ];
     uint64_t upre[kSelQ];
     uint32_t r_wtot[2][kSelWarps];
-    uint32_t tpre[kSelQ][kSelG][kSelRole];  // count before each thread within its unit
+    uint32_t tpre[kSelQ][kSelG][kSelRole];   // count before each thread within its unit
+    uint32_t tmask[kSelQ][kSelG][kSelRole];  // each thread's flags, bit e = item e
 };
 
 template <typename V>
 constexpr size_t sel_smem_bytes() {
     constexpr size_t TILE = SelShape<V>::kTile;
-    return kSelRS * TILE + kSelSS * (TILE * sizeof(V) + TILE) + TILE * sizeof(V) + sizeof(SelCtrl<V>);
+    return kSelRS * TILE + kSelSS * TILE * sizeof(V) + kSelWarps * SelShape<V>::kSlice * sizeof(V) +
+           sizeof(SelCtrl<V>);
 }
 
 struct SelArgs {
@@ -102,9 +107,8 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* rflags = smem_raw;
     V* svals = reinterpret_cast<V*>(rflags + static_cast<size_t>(RS) * TILE);
-    uint8_t* sflags = reinterpret_cast<uint8_t*>(svals + static_cast<size_t>(SS) * TILE);
-    V* ostage = reinterpret_cast<V*>(sflags + static_cast<size_t>(SS) * TILE);
-    Ctrl* ctrl = reinterpret_cast<Ctrl*>(ostage + TILE);
+    V* ostage = svals + static_cast<size_t>(SS) * TILE;
+    Ctrl* ctrl = reinterpret_cast<Ctrl*>(ostage + kSelWarps * Sh::kSlice);
 
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5;
@@ -122,7 +126,7 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
         }
         for (int q = 0; q < Q; ++q) {
             ptx::mbar_init(&ctrl->uknown[q], 1);
-            ptx::mbar_init(&ctrl->ureduced[q], 1);
+            ptx::mbar_init(&ctrl->ureduced[q], kSelWarps);
             ptx::mbar_init(&ctrl->uprefix[q], 1);
             ptx::mbar_init(&ctrl->ufree[q], kSelWarps);
         }
@@ -266,15 +270,11 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
                     ctrl->s_tile[s] = t;
                     const uint32_t cnt = count_of(t);
                     const uint32_t vbytes = (cnt * static_cast<uint32_t>(sizeof(V))) & ~15u;
-                    const uint32_t fbytes = cnt & ~15u;
-                    ptx::mbar_arrive_expect_tx(&ctrl->sfull[s], vbytes + fbytes);
+                    ptx::mbar_arrive_expect_tx(&ctrl->sfull[s], vbytes);
                     if (vbytes)
                         ptx::bulk_load_hint(svals + static_cast<size_t>(s) * TILE,
                                             static_cast<const V*>(a.in) + static_cast<uint64_t>(t) * TILE, vbytes,
                                             &ctrl->sfull[s], pol);
-                    if (fbytes)
-                        ptx::bulk_load_hint(sflags + static_cast<size_t>(s) * TILE,
-                                            sa.flags + static_cast<uint64_t>(t) * TILE, fbytes, &ctrl->sfull[s], pol);
                 }
                 if (end) break;
             }
@@ -347,9 +347,8 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
             const bool ok = wait1(&ctrl->rfull[s], (rn / RS) & 1u, long_budget);
             const uint32_t t = ok ? ctrl->r_tile[s] : kTileEnd;
             const bool live = t != kTileEnd;
-            const uint32_t cnt = live ? static_cast<uint32_t>(__popc(flag_mask(rflags + static_cast<size_t>(s) * TILE,
-                                                                               t, r)))
-                                      : 0u;
+            const uint32_t m = live ? flag_mask(rflags + static_cast<size_t>(s) * TILE, t, r) : 0u;
+            const uint32_t cnt = static_cast<uint32_t>(__popc(m));
             const uint32_t winc = warp_inclusive_scan(cnt, lane);
             if (lane == 31) ctrl->r_wtot[rn & 1u][rw] = winc;
             const bool stop = named_bar_or(1, kSelRole, !live || !ok);
@@ -369,12 +368,17 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
                 tot += x;
             }
             ctrl->tpre[q][k][r] = unit_cnt + wpre + (winc - cnt);
+            ctrl->tmask[q][k][r] = m;
             unit_cnt += tot;
             if (k == G - 1) {
-                if (r == 0) {
-                    const uint32_t u = t / G;
-                    D::store(desc + u, D::pack(u == 0 ? kInclusive : kAggregate, epoch, unit_cnt));
-                    ctrl->uagg[q] = unit_cnt;
+                // Each reduce warp releases its unit's prefixes and masks.
+                __syncwarp();
+                if (lane == 0) {
+                    if (r == 0) {
+                        const uint32_t u = t / G;
+                        D::store(desc + u, D::pack(u == 0 ? kInclusive : kAggregate, epoch, unit_cnt));
+                        ctrl->uagg[q] = unit_cnt;
+                    }
                     ptx::mbar_arrive(&ctrl->ureduced[q]);
                 }
                 unit_cnt = 0;
@@ -384,18 +388,20 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
     // ======================================================== finalize
     // Thread f owns row f of each tile (ITEMS consecutive elements), so warp
     // w owns the 32 * ITEMS consecutive elements of rows 32w .. 32w + 31 and
-    // compacts them into its own slice of the staging tile: each thread puts
-    // its selected values at its count-prefix within the warp (from the reduce
-    // pass), then the warp copies its run out with consecutive lanes on
-    // consecutive output elements. Only the warp synchronises, no barrier
-    // between the finalize warps. (A staging tile shared by the four warps
-    // needed three barriers per tile; ranking the warp's elements 32 at a
-    // time by ballots ran a dependent chain per step and was 2x slower.)
+    // compacts them into its own staging slice: each thread puts its selected
+    // values at its count-prefix within the warp (from the reduce pass), then
+    // the warp copies its run out with 16-byte stores (the run is staged at
+    // the 16-byte phase of its destination). Only the warp synchronises, no
+    // barrier between the finalize warps. The reduce pass's mask is turned
+    // into register order once (the row's chunks sit rotated in registers),
+    // so that every item tests a bit fixed at compile time, and each chunk's
+    // first position comes from one population count: no dependent chain
+    // longer than a chunk.
     else {
         const uint32_t f = tid - kWarpFinal * 32;
         const uint32_t fw = warp - kWarpFinal;
         const uint32_t rot = f & 7u;
-        V* wst = ostage + fw * 32u * ITEMS;  // this warp's staging slice
+        V* wst = ostage + fw * Sh::kSlice;  // this warp's staging slice
         uint64_t run = 0;  // the unit's output position
         for (uint32_t sn = 0;; ++sn) {
             const int s = static_cast<int>(sn % SS);
@@ -429,7 +435,6 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
                     v[e] = li < bulk ? vb[li] : (li < cnt ? g[li] : V(0));
                 }
             }
-            const uint32_t mask = flag_mask(sflags + static_cast<size_t>(s) * TILE, t, f);
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&ctrl->sfree[s]);  // this warp is done with the stage
             if (k == 0) {
@@ -438,35 +443,40 @@ __global__ void __launch_bounds__(kSelThreads, 1) select_kernel(const ScanArgs a
                 if (!pok && lane == 0) raise_error(a.hdr, kErrPipelineTimeout);
                 run = ctrl->upre[q];
             }
-            // Selected items of each register chunk, and where each chunk's
-            // run starts in logical order within the thread.
+            const uint32_t mask = ctrl->tmask[q][k][f];  // bit e: logical item e
             const uint32_t rrot = full_tile ? rot : 0u;
-            uint32_t cs[CHUNKS];
-#pragma unroll
-            for (int c8 = 0; c8 < CHUNKS; ++c8) {
-                const uint32_t l = (c8 + rrot) & (CHUNKS - 1);
-                cs[c8] = static_cast<uint32_t>(__popc((mask >> (l * EPC)) & ((1u << EPC) - 1u)));
-            }
-            uint32_t cpre[CHUNKS];
-            uint32_t total;
-            rotated_chunk_prefix<uint32_t, CHUNKS>(cs, rrot, cpre, total);
+            // The mask in register order: bit c8 * EPC + e is v[c8 * EPC + e].
+            const uint64_t m2 = mask | (static_cast<uint64_t>(mask) << ITEMS);
+            const uint32_t rm = static_cast<uint32_t>(m2 >> (rrot * EPC));
             const uint32_t warp_base = ctrl->tpre[q][k][fw * 32u];
             const uint32_t mine = ctrl->tpre[q][k][f] - warp_base;
-            const uint32_t warp_cnt = __shfl_sync(kFullMask, mine + total, 31);
+            const uint32_t warp_cnt = __shfl_sync(kFullMask, mine + static_cast<uint32_t>(__popc(mask)), 31);
+            V* out = static_cast<V*>(a.out) + run + warp_base;
+            // The run's first element goes to slot o of the slice, o being its
+            // destination's element phase within 16 bytes.
+            const uint32_t o = static_cast<uint32_t>(reinterpret_cast<uintptr_t>(out) / sizeof(V)) & (EPC - 1);
             // The slice may still be read by this warp's previous copy-out.
             __syncwarp();
 #pragma unroll
             for (int c8 = 0; c8 < CHUNKS; ++c8) {
                 const uint32_t l = (c8 + rrot) & (CHUNKS - 1);
-                uint32_t pos = mine + cpre[c8];
+                uint32_t pos = o + mine + static_cast<uint32_t>(__popc(mask & ((1u << (l * EPC)) - 1u)));
 #pragma unroll
                 for (int e = 0; e < EPC; ++e) {
-                    if ((mask >> (l * EPC + e)) & 1u) wst[pos++] = v[c8 * EPC + e];
+                    if ((rm >> (c8 * EPC + e)) & 1u) wst[pos++] = v[c8 * EPC + e];
                 }
             }
             __syncwarp();
-            V* out = static_cast<V*>(a.out) + run + warp_base;
-            for (uint32_t x = lane; x < warp_cnt; x += 32u) out[x] = wst[x];
+            // Copy-out: single elements up to the first 16-byte boundary, then
+            // 16-byte chunks, then single elements.
+            const uint32_t head = min(warp_cnt, (EPC - o) & (EPC - 1));
+            const uint32_t body = (warp_cnt - head) / EPC;
+            const uint32_t tail = head + body * EPC;
+            if (lane < head) out[lane] = wst[o + lane];
+            const Chunk<V>* src = reinterpret_cast<const Chunk<V>*>(wst + o + head);
+            Chunk<V>* dst = reinterpret_cast<Chunk<V>*>(out + head);
+            for (uint32_t x = lane; x < body; x += 32u) dst[x] = src[x];
+            if (tail + lane < warp_cnt) out[tail + lane] = wst[o + tail + lane];
             if (k == G - 1 && lane == 0) ptx::mbar_arrive(&ctrl->ufree[q]);
         }
     }
