@@ -315,7 +315,8 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     const size_t region16 = (main_bytes + 255) & ~static_cast<size_t>(255);
     const size_t end16 = slots16 ? region16 + kHeaderBytes + slots16 * 16 : main_bytes;
     const size_t region_mid = (end16 + 255) & ~static_cast<size_t>(255);
-    p->scratch_bytes = slots_mid ? region_mid + (slots_mid + groups_mid) * 16 : end16;
+    const uint64_t words_mid = slots_mid ? gps::mid_desc_words(tiles) : 0;
+    p->scratch_bytes = slots_mid ? region_mid + (words_mid + groups_mid) * 16 : end16;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;
@@ -330,7 +331,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     if (algo == GPS_ALGO_CSDL)
         p->group_desc16 = static_cast<char*>(p->desc16) + (tiles + gps::kDescPad) * (slots16 ? 16 : per_tile);
     p->desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid : nullptr;
-    p->group_desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid + slots_mid * 16 : nullptr;
+    p->group_desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid + words_mid * 16 : nullptr;
     gps::WsHeader h{};
     h.epoch = 1;
     h.capacity_tiles = slots;

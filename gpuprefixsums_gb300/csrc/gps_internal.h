@@ -79,7 +79,7 @@ struct ScanArgs {
     void* out;
     uint64_t n;
     uint32_t num_tiles;
-    uint32_t pad_;
+    uint32_t desc_stride;  // one-tile-per-CTA kernels: 16-byte words between tile descriptors
     WsHeader* hdr;       // plan state (counters, epoch, error flags)
     void* desc;          // tile descriptors (lookback)
     // Descriptors of groups: of 32 tiles for the one-tile-per-CTA kernels, of
@@ -204,6 +204,19 @@ cudaError_t launch_small(gps_dtype dtype, bool inclusive, const ScanArgs& a, cud
 // u64: 25.4 against 26.8 us at 3 x 2^21), slower at 64 MB (u32: 37.4 against
 // 34.6 us at 2^24; u64: 38.4 against 32.7 us at 2^23).
 constexpr size_t kMidMaxBytes = 48ull << 20;
+// Tile descriptors of the one-tile-per-CTA kernels sit one per 128-byte line
+// (a stride of 8 words) when a launch has more than one group of 32 tiles
+// and at most kMidStrideMaxTiles tiles, else packed. Sharing lines between
+// tiles that publish and read at the same moment cost up to 3 us per read
+// (2^20 u32: 6.04 us packed, 4.95 us one per line, 5.23 us one per 32-byte
+// sector); with one group, packed reads are faster (2^17: 2.83 against
+// 3.36 us). Descriptor words a plan keeps for `tiles` tiles:
+constexpr uint32_t kMidDescStride = 8;
+constexpr uint64_t kMidStrideMaxTiles = 4096;
+constexpr uint64_t mid_desc_words(uint64_t tiles) {
+    const uint64_t strided = ((tiles < kMidStrideMaxTiles ? tiles : kMidStrideMaxTiles) + kDescPad) * kMidDescStride;
+    return tiles + kDescPad > strided ? tiles + kDescPad : strided;
+}
 cudaError_t launch_mid(gps_dtype dtype, bool inclusive, const ScanArgs& a, int num_sms, cudaStream_t stream,
                        LaunchInfo* info);
 

@@ -36,7 +36,10 @@ constexpr int kMidVecCtasPerSm = 8;
 // ------------------------------------------------------------ descriptors
 // One 16-byte word per tile: {lo: the value (u32 or u64), hi: status:2 |
 // grid id:62}. Zeroed memory reads "not ready". 2^62 launches would have to
-// pass in one context before a stale tag could come round again.
+// pass in one context before a stale tag could come round again. Tile t's
+// word is word t * a.desc_stride of the region: launches of more than one
+// group of tiles give each tile a 128-byte line of its own, since tiles that
+// publish while others read the same line waited up to 3 us for a read.
 constexpr uint64_t kGidMask = (1ull << 62) - 1;
 
 struct MidDesc {
@@ -84,8 +87,8 @@ struct LookbackSmem {
 // whether an inclusive one was found and, in `sum`, the sum of those slots.
 // Gives up after the wait budget, setting timed_out (then `sum` is 0).
 template <typename T, uint32_t SPIN = 64>
-__device__ bool warp_window(const ScanArgs& a, const ptx::u64x2* d, int64_t top, int64_t floor, uint64_t gid,
-                            uint32_t lane, T& sum, bool& timed_out) {
+__device__ bool warp_window(const ScanArgs& a, const ptx::u64x2* d, uint32_t stride, int64_t top, int64_t floor,
+                            uint64_t gid, uint32_t lane, T& sum, bool& timed_out) {
     const int64_t idx = top - static_cast<int64_t>(lane);
     bool ready = idx < floor, incl = false;
     T v = 0;
@@ -94,7 +97,7 @@ __device__ bool warp_window(const ScanArgs& a, const ptx::u64x2* d, int64_t top,
     timed_out = false;
     while (true) {
         if (!ready) {
-            const ptx::u64x2 w = ptx::ld_relaxed_b128(d + idx);
+            const ptx::u64x2 w = ptx::ld_relaxed_b128(d + idx * stride);
             const uint32_t st = MidDesc::status(w, gid);
             if (st != kNotReady) {
                 ready = true;
@@ -140,6 +143,7 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
                                              T* s_pre) {
     ptx::u64x2* d1 = static_cast<ptx::u64x2*>(a.desc);
     ptx::u64x2* d2 = static_cast<ptx::u64x2*>(a.group_desc);
+    const uint32_t s1 = a.desc_stride;
     const T carry = a.carry_in != nullptr ? *static_cast<const T*>(a.carry_in) : T(0);
     const uint32_t tid = threadIdx.x;
     const uint32_t g = t / kGroupTiles;
@@ -153,13 +157,14 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
     }
     if (tid < 32) {
         const uint32_t lane = tid;
-        if (lane == 0) ptx::st_relaxed_b128(d1 + t, MidDesc::pack(kAggregate, gid, static_cast<uint64_t>(total)));
+        if (lane == 0)
+            ptx::st_relaxed_b128(d1 + t * s1, MidDesc::pack(kAggregate, gid, static_cast<uint64_t>(total)));
         // The tiles of this group before t; tile 0 is inclusive, so group 0
         // always finds one.
         T in_sum;
         bool timed_out;
-        const bool found = warp_window<T>(a, d1, static_cast<int64_t>(t) - 1, static_cast<int64_t>(g) * kGroupTiles,
-                                          gid, lane, in_sum, timed_out);
+        const bool found = warp_window<T>(a, d1, s1, static_cast<int64_t>(t) - 1,
+                                          static_cast<int64_t>(g) * kGroupTiles, gid, lane, in_sum, timed_out);
         if (lane == 0 && group_last && !timed_out)
             ptx::st_relaxed_b128(d2 + g, MidDesc::pack(found ? kInclusive : kAggregate, gid,
                                                        static_cast<uint64_t>(in_sum + total)));
@@ -170,7 +175,7 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
             int64_t top = static_cast<int64_t>(g) - 1;
             while (true) {
                 T part;
-                const bool gf = warp_window<T>(a, d2, top, 0, gid, lane, part, timed_out);
+                const bool gf = warp_window<T>(a, d2, 1, top, 0, gid, lane, part, timed_out);
                 if (timed_out) break;
                 gsum += part;
                 if (gf || top < 32) break;  // group 0's descriptor is inclusive
@@ -190,7 +195,7 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
     }
     const T pre = s_pre[0];
     if (tid == 0) {
-        ptx::st_relaxed_b128(d1 + t, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
+        ptx::st_relaxed_b128(d1 + t * s1, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
         if (group_last && sm.found == 0)
             ptx::st_relaxed_b128(d2 + g, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
         if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
@@ -358,8 +363,10 @@ __global__ void __launch_bounds__(kMidThreads, kMidVecCtasPerSm) mid_vec_kernel(
 }
 
 template <typename T, bool INCL, bool VEC>
-cudaError_t launch_mid_v(const ScanArgs& a, cudaStream_t stream, LaunchInfo* info) {
+cudaError_t launch_mid_v(const ScanArgs& a0, cudaStream_t stream, LaunchInfo* info) {
     auto kern = VEC ? mid_vec_kernel<T, INCL> : mid_scan_kernel<T, INCL>;
+    ScanArgs a = a0;
+    a.desc_stride = a.num_tiles > kGroupTiles && a.num_tiles <= kMidStrideMaxTiles ? kMidDescStride : 1u;
     const int grid = static_cast<int>(a.num_tiles);
     if (info) *info = LaunchInfo{grid, kMidThreads, 0};
     kern<<<grid, kMidThreads, 0, stream>>>(a);
