@@ -451,7 +451,7 @@ def run_sweep(stream, d_in, d_out):
     second power of two) on the benchmark's buffers, beside CUB DeviceScan on
     the same buffers, and u64 at n = 2^27. GPU time per scan from CUDA-graph
     replay. Inputs below about 2^24 elements stay in L2 between launches.
-    The plan's defaults pick the kernel: one tile per CTA up to 48 MB, the
+    The plan's defaults pick the kernel: one tile per CTA up to 64 MB, the
     persistent L2-buffered kernel above."""
     import torch
 

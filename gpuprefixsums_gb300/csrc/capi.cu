@@ -316,7 +316,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     const size_t end16 = slots16 ? region16 + kHeaderBytes + slots16 * 16 : main_bytes;
     const size_t region_mid = (end16 + 255) & ~static_cast<size_t>(255);
     const uint64_t words_mid = slots_mid ? gps::mid_desc_words(tiles) : 0;
-    p->scratch_bytes = slots_mid ? region_mid + (words_mid + groups_mid) * 16 : end16;
+    p->scratch_bytes = slots_mid ? region_mid + (words_mid + groups_mid * gps::kMidDescStride) * 16 : end16;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
         delete p;

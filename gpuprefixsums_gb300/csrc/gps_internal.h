@@ -199,18 +199,21 @@ cudaError_t launch_small(gps_dtype dtype, bool inclusive, const ScanArgs& a, cud
 
 // Integer chained scans up to mid size, one 16 KB tile per CTA (mid.cu); the
 // default upper size of a plan, in bytes of input. Measured on GB300 (graph
-// replay, L2-resident buffers): one tile per CTA is faster than the
-// persistent kernel up to 48 MB (u32: 13.0 against 16.5 us at 3 x 2^22;
-// u64: 25.4 against 26.8 us at 3 x 2^21), slower at 64 MB (u32: 37.4 against
-// 34.6 us at 2^24; u64: 38.4 against 32.7 us at 2^23).
-constexpr size_t kMidMaxBytes = 48ull << 20;
+// replay; descriptors one per line): one tile per CTA is faster than the
+// persistent kernel up to 64 MB (u32: 31.8 against 34.4 us at 2^24; u64:
+// 32.1 against 32.8 us at 2^23), slower from 96 MB (u32: 43.7 against 44.6
+// us at 3 x 2^23 at best, 56.5 against 53.7 at 2^25; u64: 44.5 against 43.2
+// at 3 x 2^22).
+constexpr size_t kMidMaxBytes = 64ull << 20;
 // Tile descriptors of the one-tile-per-CTA kernels sit one per 128-byte line
 // (a stride of 8 words) when a launch has more than one group of 32 tiles
 // and at most kMidStrideMaxTiles tiles, else packed. Sharing lines between
 // tiles that publish and read at the same moment cost up to 3 us per read
 // (2^20 u32: 6.04 us packed, 4.95 us one per line, 5.23 us one per 32-byte
 // sector); with one group, packed reads are faster (2^17: 2.83 against
-// 3.36 us). Descriptor words a plan keeps for `tiles` tiles:
+// 3.36 us). Group descriptors always take a line each (2^22 u32: 7.56
+// against 8.84 us packed). Tile-descriptor words a plan keeps for `tiles`
+// tiles:
 constexpr uint32_t kMidDescStride = 8;
 constexpr uint64_t kMidStrideMaxTiles = 4096;
 constexpr uint64_t mid_desc_words(uint64_t tiles) {

@@ -40,6 +40,7 @@ constexpr int kMidVecCtasPerSm = 8;
 // word is word t * a.desc_stride of the region: launches of more than one
 // group of tiles give each tile a 128-byte line of its own, since tiles that
 // publish while others read the same line waited up to 3 us for a read.
+// Group descriptors always have a line each (word g * kMidDescStride).
 constexpr uint64_t kGidMask = (1ull << 62) - 1;
 
 struct MidDesc {
@@ -166,7 +167,7 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
         const bool found = warp_window<T>(a, d1, s1, static_cast<int64_t>(t) - 1,
                                           static_cast<int64_t>(g) * kGroupTiles, gid, lane, in_sum, timed_out);
         if (lane == 0 && group_last && !timed_out)
-            ptx::st_relaxed_b128(d2 + g, MidDesc::pack(found ? kInclusive : kAggregate, gid,
+            ptx::st_relaxed_b128(d2 + g * kMidDescStride, MidDesc::pack(found ? kInclusive : kAggregate, gid,
                                                        static_cast<uint64_t>(in_sum + total)));
         // No inclusive tile in the group before t: the prefix of the group, a
         // decoupled lookback over the group descriptors, 32 per poll.
@@ -175,7 +176,7 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
             int64_t top = static_cast<int64_t>(g) - 1;
             while (true) {
                 T part;
-                const bool gf = warp_window<T>(a, d2, 1, top, 0, gid, lane, part, timed_out);
+                const bool gf = warp_window<T>(a, d2, kMidDescStride, top, 0, gid, lane, part, timed_out);
                 if (timed_out) break;
                 gsum += part;
                 if (gf || top < 32) break;  // group 0's descriptor is inclusive
@@ -197,7 +198,7 @@ __device__ __forceinline__ T mid_tile_prefix(const ScanArgs& a, uint32_t t, uint
     if (tid == 0) {
         ptx::st_relaxed_b128(d1 + t * s1, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
         if (group_last && sm.found == 0)
-            ptx::st_relaxed_b128(d2 + g, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
+            ptx::st_relaxed_b128(d2 + g * kMidDescStride, MidDesc::pack(kInclusive, gid, static_cast<uint64_t>(pre + total)));
         if (a.carry_out != nullptr && t == a.num_tiles - 1) *static_cast<T*>(a.carry_out) = pre + total;
     }
     return pre;

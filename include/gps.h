@@ -246,8 +246,8 @@ gps_status gps_plan_set_fallback(gps_plan plan, uint32_t fallback_polls);
 gps_status gps_plan_set_small_max(gps_plan plan, uint64_t max_n);
 
 /* Integer scans on a GPS_ALGO_CSDL plan above the one-CTA size and of at
- * most max_n elements (default: 48 MB of input, 12 x 2^20 u32 or 6 x 2^20
- * u64) run as one 16 KB tile per CTA -- a single-pass chained scan without
+ * most max_n elements (default: 64 MB of input, 2^24 u32 or 2^23 u64) run
+ * as one 16 KB tile per CTA -- a single-pass chained scan without
  * the persistent kernel's pipeline, whose latency dominates at these sizes;
  * larger ones run on the persistent L2-buffered kernel. 0 sends them all to
  * the persistent kernel. Forced-stall and fallback modes always use the
