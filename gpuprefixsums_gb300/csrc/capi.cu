@@ -29,14 +29,15 @@ inline int size_class(uint64_t n) {
     return std::min(kSizeClasses - 1, bits / 2);
 }
 
-// Staging buffers of gps_scan_host, and their size in bytes (at most): four
-// chunks of 16 MB keep copies in both directions and the scans going at once.
+// Staging buffers of gps_scan_host, and their size in bytes (at most): six
+// chunks of 32 MB keep copies in both directions and the scans going at once.
 // Measured on GB300 with 1 GiB each way (pinned): either direction alone
 // takes 5.09 / 5.56 ms, both at once 6.28 ms (the host link does not carry
-// both at full rate). The scan of the array takes 7.01 ms with four 16 MB
-// chunks, 7.16 ms with two of 64 MB.
-constexpr int kHostStages = 4;
-constexpr uint64_t kHostChunkBytes = 16ull << 20;
+// both at full rate). The scan of the array takes 6.76-6.89 ms with six
+// 32 MB chunks, 6.73-6.93 with four of 64 MB, 7.01-7.04 with four of 16 MB,
+// 7.5 with eight of 8 MB, 7.16 with two of 64 MB.
+constexpr int kHostStages = 6;
+constexpr uint64_t kHostChunkBytes = 32ull << 20;
 
 struct gps_plan_s {
     gps_algo algo;
@@ -630,7 +631,7 @@ gps_status gps_scan_host(gps_plan p, gps_scan_kind kind, const void* h_in, void*
     const size_t es = gps::dtype_size(p->dtype);
     cudaError_t err = cudaSuccess;
     if (p->stage[0] == nullptr) {
-        // Chunk: up to 16 MB, whole tiles, within the plan's size.
+        // Chunk: up to kHostChunkBytes, whole tiles, within the plan's size.
         uint64_t chunk = std::min<uint64_t>(p->max_n, kHostChunkBytes / es);
         if (chunk > p->tile_elems) chunk -= chunk % p->tile_elems;
         for (int b = 0; b < kHostStages && err == cudaSuccess; ++b) err = cudaMalloc(&p->stage[b], chunk * es);

@@ -196,7 +196,7 @@ gps_status gps_plan_set_generic_config(gps_plan plan, int segmented, uint64_t n,
  * scans; returns when h_out is complete (synchronizes `stream`). Host buffers
  * should be pinned (cudaHostAlloc / cudaHostRegister) for full speed; h_in ==
  * h_out is allowed. n may exceed the plan's max_n: the plan only bounds the
- * chunk size. Device staging memory (four chunks of up to 16 MB) is
+ * chunk size. Device staging memory (six chunks of up to 32 MB) is
  * allocated on first use and kept by the plan. u32 and u64 plans (others: GPS_ERR_UNSUPPORTED). */
 gps_status gps_scan_host(gps_plan plan, gps_scan_kind kind, const void* h_in, void* h_out,
                          uint64_t n, gps_stream_t stream);

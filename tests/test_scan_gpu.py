@@ -194,7 +194,7 @@ def test_config2_exclusive_sweep_2pow10_to_2pow28(cuda, dist):
 @pytest.mark.parametrize("inclusive", [False, True])
 @pytest.mark.parametrize("path", ["mid", "persistent"])
 def test_host_array_scan_chunks_and_carries(cuda, algo, inclusive, path):
-    n = (1 << 23) + 12345  # the plan's 2^21 bound forces five chunks
+    n = (1 << 24) + 12345  # the plan's 2^21 bound forces nine chunks: the six staging buffers wrap
     x = rand("u32", n, seed=5)
     h_in = torch.from_numpy(x.view(np.int32)).pin_memory()
     h_out = torch.empty(n, dtype=torch.int32).pin_memory()
