@@ -294,17 +294,19 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     }
     // Chained scan: one descriptor per tile plus the lookback padding;
     // reduce-then-scan: one tile sum per tile.
-    // Generic-kernel descriptors are followed by the group descriptors of its
-    // lookback (one per kDetGroupUnits single-tile units, and a spare).
+    // Generic-kernel descriptors (packed, or one per line for launches of few
+    // units) are followed by the group descriptors of its lookback; both are
+    // counted in 16-byte words.
     const size_t per_tile = algo == GPS_ALGO_CSDL ? desc_bytes(dtype) : gps::dtype_size(dtype);
-    const uint64_t det_groups = gps::det_group_slots(tiles);
-    const uint64_t slots =
-        algo == GPS_ALGO_CSDL ? tiles + gps::kDescPad + (dtype != GPS_DTYPE_U32 ? det_groups : 0) : tiles;
+    const uint64_t seg_dw = (dtype == GPS_DTYPE_U32 ? 16 : per_tile) / 16;  // words per generic descriptor
+    const uint64_t seg_units = gps::seg_desc_words(tiles, seg_dw), seg_groups = gps::seg_group_words(tiles, seg_dw);
+    const uint64_t slots = algo == GPS_ALGO_CSDL ? (dtype != GPS_DTYPE_U32 ? (seg_units + seg_groups) / seg_dw
+                                                                          : tiles + gps::kDescPad)
+                                                 : tiles;
     // u32 chained-scan plans keep 8-byte descriptors; batched scans of them
     // use the generic kernel's 16-byte descriptors, kept in a region of their
     // own so that the two formats never meet in one slot.
-    const uint64_t slots16 =
-        (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? tiles + gps::kDescPad + det_groups : 0;
+    const uint64_t slots16 = (algo == GPS_ALGO_CSDL && dtype == GPS_DTYPE_U32) ? seg_units + seg_groups : 0;
     // One-tile-per-CTA kernels of integer chained-scan plans: 16-byte
     // descriptors tagged with the launch, in a region no other kernel uses.
     const uint64_t slots_mid = (algo == GPS_ALGO_CSDL && !generic_only(dtype)) ? tiles + gps::kDescPad : 0;
@@ -329,8 +331,7 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->area = static_cast<char*>(p->scratch) + kHeaderBytes + kCarryBytes;
     p->hdr16 = slots16 ? reinterpret_cast<gps::WsHeader*>(static_cast<char*>(p->scratch) + region16) : p->hdr;
     p->desc16 = slots16 ? static_cast<char*>(p->scratch) + region16 + kHeaderBytes : p->area;
-    if (algo == GPS_ALGO_CSDL)
-        p->group_desc16 = static_cast<char*>(p->desc16) + (tiles + gps::kDescPad) * (slots16 ? 16 : per_tile);
+    if (algo == GPS_ALGO_CSDL) p->group_desc16 = static_cast<char*>(p->desc16) + seg_units * 16;
     p->desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid : nullptr;
     p->group_desc_mid = slots_mid ? static_cast<char*>(p->scratch) + region_mid + words_mid * 16 : nullptr;
     gps::WsHeader h{};

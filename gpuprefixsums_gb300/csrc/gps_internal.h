@@ -74,12 +74,35 @@ enum class PrefixMode : int { Lookback = 0, Spine = 1 };
 constexpr uint32_t kDetGroupUnits = 128;
 constexpr uint64_t det_group_slots(uint64_t units) { return (units + kDetGroupUnits - 1) / kDetGroupUnits + 1; }
 
+// The generic kernel's unit and group descriptors sit one per 128-byte line
+// (a stride of 8 words) when a launch has at most kSegStrideMaxUnits
+// lookback units, else packed (Op::kDescWords words each). Measured on GB300
+// (FP32, GPU time per scan): one per line 11.6 against 12.4 us at 2^20, 14.9
+// against 15.7 at 2^22, 29.0 against 31.7 at 2^24 (1024 units of 4 tiles);
+// packed 91 against 94 us at 2^26 and 173 against 178 at 2^27, where the
+// wider reads compete with the data for L2. 16-byte words a plan keeps for
+// up to `tiles` units of `dw` words, and for their group descriptors:
+constexpr uint32_t kSegDescStride = 8;
+constexpr uint64_t kSegStrideMaxUnits = 1024;
+constexpr uint64_t seg_desc_words(uint64_t tiles, uint64_t dw) {
+    const uint64_t packed = (tiles + kDescPad) * dw;
+    const uint64_t strided = ((tiles < kSegStrideMaxUnits ? tiles : kSegStrideMaxUnits) + kDescPad) * kSegDescStride;
+    return packed > strided ? packed : strided;
+}
+constexpr uint64_t seg_group_words(uint64_t tiles, uint64_t dw) {
+    const uint64_t packed = det_group_slots(tiles) * dw;
+    const uint64_t strided = det_group_slots(tiles < kSegStrideMaxUnits ? tiles : kSegStrideMaxUnits) * kSegDescStride;
+    return packed > strided ? packed : strided;
+}
+
 struct ScanArgs {
     const void* in;
     void* out;
     uint64_t n;
     uint32_t num_tiles;
-    uint32_t desc_stride;  // one-tile-per-CTA kernels: 16-byte words between tile descriptors
+    // One-tile-per-CTA and generic kernels: 16-byte words from one descriptor
+    // to the next (0: packed), set by their launchers.
+    uint32_t desc_stride;
     WsHeader* hdr;       // plan state (counters, epoch, error flags)
     void* desc;          // tile descriptors (lookback)
     // Descriptors of groups: of 32 tiles for the one-tile-per-CTA kernels, of

@@ -100,27 +100,34 @@ __device__ __forceinline__ void thread_outputs(typename Op::T (&v)[ITEMS], typen
     }
 }
 
+// Words from one unit descriptor (or group descriptor) to the next.
+template <class Op>
+__device__ __forceinline__ uint32_t desc_words(const ScanArgs& a) {
+    return a.desc_stride != 0 ? a.desc_stride : static_cast<uint32_t>(Op::kDescWords);
+}
+
 // A unit's descriptor is Op::kDescWords 128-bit words, each carrying one
 // 64-bit word of the chain value with the status, head flag and epoch: a
 // reader takes the value only when every word has the launch's epoch and
 // the same status (a word that is one publication behind reads as not
-// ready).
+// ready). Descriptor u starts at word u * ws: ws is Op::kDescWords (packed)
+// or a.desc_stride (one 128-byte line per descriptor, see desc_words()).
 template <class Op>
-__device__ __forceinline__ void desc_store(ptx::u64x2* desc, uint64_t u, uint32_t status, bool flag, uint32_t epoch,
-                                           typename Op::C c) {
+__device__ __forceinline__ void desc_store(ptx::u64x2* desc, uint64_t u, uint32_t ws, uint32_t status, bool flag,
+                                           uint32_t epoch, typename Op::C c) {
 #pragma unroll
     for (int w = 0; w < Op::kDescWords; ++w)
-        ptx::st_relaxed_b128(desc + u * Op::kDescWords + w, seg_pack(status, flag, epoch, Op::chain_word(c, w)));
+        ptx::st_relaxed_b128(desc + u * ws + w, seg_pack(status, flag, epoch, Op::chain_word(c, w)));
 }
 
 template <class Op>
-__device__ __forceinline__ uint32_t desc_load(const ptx::u64x2* desc, uint64_t u, uint32_t epoch, bool& flag,
-                                              typename Op::C& c) {
+__device__ __forceinline__ uint32_t desc_load(const ptx::u64x2* desc, uint64_t u, uint32_t ws, uint32_t epoch,
+                                              bool& flag, typename Op::C& c) {
     uint64_t words[Op::kDescWords];
     uint32_t st = kNotReady;
 #pragma unroll
     for (int w = 0; w < Op::kDescWords; ++w) {
-        const ptx::u64x2 x = ptx::ld_relaxed_b128(desc + u * Op::kDescWords + w);
+        const ptx::u64x2 x = ptx::ld_relaxed_b128(desc + u * ws + w);
         const uint32_t s = (static_cast<uint32_t>(x.hi) & kEpochMask) == (epoch & kEpochMask)
                                ? static_cast<uint32_t>(x.hi >> 62)
                                : kNotReady;
@@ -166,6 +173,7 @@ static_assert(kDetGroupUnits % 32 == 0 && kDetGroupUnits <= 32 * 32, "whole lane
 template <class Op>
 __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t epoch, uint32_t lane) {
     using C = typename Op::C;
+    const uint32_t ws = desc_words<Op>(a);
     constexpr int K = static_cast<int>(kDetGroupUnits / 32);  // units per lane
     const ptx::u64x2* desc = static_cast<const ptx::u64x2*>(a.desc);
     const ptx::u64x2* gdesc = static_cast<const ptx::u64x2*>(a.group_desc);
@@ -206,7 +214,7 @@ __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t e
             if (!((ready >> j) & 1u)) {
                 bool hf = false;
                 C cv;
-                if (desc_load<Op>(desc, i0 + lane * K + j, epoch, hf, cv) != kNotReady) {
+                if (desc_load<Op>(desc, i0 + lane * K + j, ws, epoch, hf, cv) != kNotReady) {
                     v[j] = cv;
                     f[j] = hf;
                     ready |= 1u << j;
@@ -240,7 +248,7 @@ __device__ typename Op::C seg_lookback(const ScanArgs& a, uint32_t u, uint32_t e
     C gp = Op::chain_zero();
     while (true) {
         bool hf = false;
-        const bool ok = desc_load<Op>(gdesc, g - 1, epoch, hf, gp) == kInclusive;
+        const bool ok = desc_load<Op>(gdesc, g - 1, ws, epoch, hf, gp) == kInclusive;
         if (__all_sync(kFullMask, ok)) break;
         if (expired()) return Op::chain_zero();
     }
@@ -726,7 +734,8 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             if (lane == 0) {
                 // The last unit of a group passes the group prefix on.
                 if ((u % kDetGroupUnits) == kDetGroupUnits - 1)
-                    desc_store<Op>(static_cast<ptx::u64x2*>(a.group_desc), u / kDetGroupUnits, kInclusive, false,
+                    desc_store<Op>(static_cast<ptx::u64x2*>(a.group_desc), u / kDetGroupUnits, desc_words<Op>(a),
+                                   kInclusive, false,
                                    epoch, incl);
                 ctrl->upre[q] = pre;
                 ptx::mbar_arrive(&ctrl->uprefix[q]);
@@ -784,7 +793,7 @@ __global__ void __launch_bounds__(SegShape<Op, RW>::kThreads, 1)
             if (lane == 0) {
                 const uint32_t u = ctrl->unit_of[q];
                 const C chain = Op::to_chain(Op::norm(unit_agg));
-                desc_store<Op>(desc, u, kAggregate, unit_flag, epoch, chain);
+                desc_store<Op>(desc, u, desc_words<Op>(a), kAggregate, unit_flag, epoch, chain);
                 ctrl->uagg[q] = chain;
                 ctrl->uflag[q] = unit_flag;
                 ptx::mbar_arrive(&ctrl->ureduced[q]);

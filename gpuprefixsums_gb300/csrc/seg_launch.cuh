@@ -56,7 +56,9 @@ cudaError_t launch_seg_t(const ScanArgs& a, const SegArgs& sg, const GenericConf
     const int ctas = std::max(1, occ * num_sms / static_cast<int>(std::max(1u, cfg.ctas_div)));
     const int grid = persistent_grid(units, 1, ctas);
     if (info) *info = LaunchInfo{grid, threads, smem};
-    kern<<<grid, threads, smem, stream>>>(a, sg, maps.in, maps.out);
+    ScanArgs b = a;
+    b.desc_stride = units <= kSegStrideMaxUnits ? kSegDescStride : 0u;
+    kern<<<grid, threads, smem, stream>>>(b, sg, maps.in, maps.out);
     return cudaGetLastError();
     }
 }
