@@ -184,6 +184,28 @@ def test_autotune_keeps_a_configuration_per_size_class(cuda):
     assert np.array_equal(got.cpu().numpy().view(np.uint32), oracle.segscan(x, offs, False))
 
 
+@pytest.mark.parametrize("unit", [1, 4])
+def test_generic_descriptor_layout_boundaries(cuda, unit):
+    # The generic kernel gives each unit descriptor a 128-byte line for
+    # launches of up to 1024 units and packs them beyond: unit counts on both
+    # sides of the limit, batched u32 (exact) on one plan.
+    rng = np.random.default_rng(61 + unit)
+    tile = 4096
+    with Plan("csdl", "u32", max_n=1100 * unit * tile) as plan:
+        for units in (1024, 1025, 1023, 129, 1100):
+            n = units * unit * tile - int(rng.integers(0, 100))
+            lengths = rng.integers(1, 3 * tile * unit, size=max(1, n // (tile * unit)))
+            lengths = np.append(lengths, 0)
+            offs = np.minimum(np.concatenate([[0], np.cumsum(lengths)]), n)
+            offs[-1] = n
+            x = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+            d_off = torch.from_numpy(offs.astype(np.uint32).view(np.int32)).cuda()
+            plan.set_generic_config(n, unit, 1)
+            got = plan.scan_segmented(dev(x), d_off, inclusive=True)
+            plan.check()
+            assert np.array_equal(got.cpu().numpy().view(np.uint32), oracle.segscan(x, offs.astype(np.uint64), True)), units
+
+
 # ------------------------------------------------------------ floating point
 def fp_errors(got, exact, x):
     got = got.astype(np.float64)

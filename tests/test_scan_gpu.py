@@ -149,6 +149,28 @@ def test_u64_2pow27(cuda, algo):
     assert oracle.validate(x, to_host(out, np.uint64), False) == 0
 
 
+# ------------------------------------- descriptor layouts at their limits
+@pytest.mark.parametrize("dtype", ["u32", "u64"])
+def test_mid_descriptor_layout_boundaries(cuda, dtype):
+    # The one-tile-per-CTA kernel packs tile descriptors 8 to a 128-byte line
+    # for launches of up to 32 tiles and gives each its own line from 33 to
+    # 4096 tiles; past 4096 (mid_max raised) they are packed again. Launches
+    # of each layout in a row on one plan, tile counts on both sides of each
+    # limit, ragged last tiles.
+    t = TILE[dtype]
+    tiles = [32, 33, 4096, 4097, 1, 2, 31, 64, 4095]
+    top = max(tiles) * t
+    with Plan("csdl", dtype, max_n=top) as plan:
+        plan.set_small_max(0)
+        plan.set_mid_max(top)
+        for k, nt in enumerate(tiles):
+            n = nt * t - (k % 3) * 7
+            x = rand(dtype, n, seed=500 + k)
+            out = plan.scan(to_dev(x), inclusive=bool(k & 1))
+            plan.check()
+            assert oracle.validate(x, to_host(out, NP[dtype]), bool(k & 1)) == 0, (dtype, nt)
+
+
 # ---------------------------------------------------------- config 2 sweep
 def _config2_sizes():
     rng = np.random.default_rng(2)
