@@ -322,9 +322,10 @@ gps_status gps_plan_create(gps_plan* out_plan, gps_algo algo, gps_dtype dtype, u
     p->scratch_bytes = slots_mid ? region_mid + (words_mid + groups_mid * gps::kMidDescStride) * 16 : end16;
     err = cudaMalloc(&p->scratch, p->scratch_bytes);
     if (err != cudaSuccess) {
+        const size_t bytes = p->scratch_bytes;
         delete p;
         return fail(err == cudaErrorMemoryAllocation ? GPS_ERR_OUT_OF_MEMORY : GPS_ERR_CUDA, "cudaMalloc(%zu): %s",
-                    p->scratch_bytes, cudaGetErrorString(err));
+                    bytes, cudaGetErrorString(err));
     }
     p->hdr = static_cast<gps::WsHeader*>(p->scratch);
     p->carries = static_cast<char*>(p->scratch) + kHeaderBytes;
