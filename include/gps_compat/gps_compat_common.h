@@ -1,9 +1,10 @@
 /*
  * Shared body of the drop-in dispatcher classes (host C++ over include/gps.h).
  *
- * The reference's dispatchers (GPUPrefixSumsCUDA/*Dispatcher.cuh) own a u32
- * buffer of maxSize elements, scan it in place, test themselves on all-ones
- * input and time themselves with CUDA events. These classes keep that public
+ * The reference's dispatchers (the *Dispatcher.cuh headers of the
+ * GPUPrefixSumsCUDA folder) own a u32 buffer of maxSize elements, scan it in
+ * place, test themselves on all-ones input and time themselves with CUDA
+ * events. These classes keep that public
  * surface -- constructor(uint32_t maxSize), TestAllExclusive(),
  * TestAllInclusive(), BatchTimingInclusive(size, batchCount), destructor --
  * and its console messages, but every scan runs through gps_scan().
@@ -60,7 +61,7 @@ class DispatcherBase {
         m_ok = true;
     }
 
-    ~DispatcherBase() { Release(); }
+    virtual ~DispatcherBase() { Release(); }
 
     void Release() {
         if (m_scan) cudaFree(m_scan);
